@@ -1,0 +1,392 @@
+"""Graph500-style BFS benchmark on one GB300 (or N replicas).
+
+Workload (default): RMAT scale 21, edgefactor 16, A/B/C/D = .57/.19/.19/.05,
+seed 0, symmetrised and deduplicated; 64 roots drawn with the Graph500 rule
+(seed 1); one direction-optimizing search per root.  A step = the 64
+searches.  Metric: harmonic-mean GTEPS over the roots, m counted with the
+reference's undirected-dedup rule (bfs_timing.py:379-398).
+
+* value: each search timed with CUDA events on the handle's stream, outputs
+  (levels + parents) left in HBM.
+* e2e: the same searches through the C ABI call cg_bfs with page-locked host
+  buffers: launch + every round + parent array copied to host memory (the
+  Graph500 Kernel-2 rule), timed on the host clock.
+* --impl reference: the reference's own host BFS (scipy breadth_first_order
+  on A^T, run_graph500.py:383-395), one search per host core in parallel.
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+# DRAM bytes per launch of bfs_persistent measured with ncu (read + write),
+# scaled per search; see profiles/bfs_persistent_rmat21.md.  None until measured.
+NCU_TRAFFIC_BYTES = None
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+  ap = argparse.ArgumentParser()
+  ap.add_argument("--gpus", type=int, default=1)
+  ap.add_argument("--steps", type=int, default=5)
+  ap.add_argument("--warmup", type=int, default=3)
+  ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+  ap.add_argument("--scale", type=int, default=21)
+  ap.add_argument("--edgefactor", type=int, default=16)
+  ap.add_argument("--seed", type=int, default=0)
+  ap.add_argument("--roots", type=int, default=64)
+  ap.add_argument("--root-seed", type=int, default=1)
+  ap.add_argument("--direction", default="auto", choices=["auto", "topdown", "bottomup", "tau"])
+  ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                  help="bound on the CPU-baseline sample")
+  ap.add_argument("--no-cpu-baseline", action="store_true")
+  return ap.parse_args()
+
+
+def dist_env():
+  rank = int(os.environ.get("RANK", "0"))
+  world = int(os.environ.get("WORLD_SIZE", "1"))
+  local = int(os.environ.get("LOCAL_RANK", "0"))
+  return rank, world, local
+
+
+def peaks():
+  path = os.path.join(HERE, "MEASURED_PEAKS.json")
+  try:
+    with open(path, encoding="utf-8") as f:
+      d = json.load(f)
+    return float(d["hbm_gbs"]), "measured"
+  except Exception:
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+  """nvidia-smi clock/throttle samples during the timed region (read only)."""
+
+  FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+            "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+            "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+  def __init__(self, gpu_index):
+    self.gpu = gpu_index
+    self.proc = None
+
+  def start(self):
+    try:
+      self.proc = subprocess.Popen(
+          ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+           "--format=csv,noheader,nounits", "-lms", "200"],
+          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+      self.proc = None
+
+  def stop(self):
+    if self.proc is None:
+      return None
+    self.proc.terminate()
+    try:
+      out, _ = self.proc.communicate(timeout=5)
+    except Exception:
+      self.proc.kill()
+      out, _ = self.proc.communicate()
+    sm, smax, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.strip().splitlines():
+      parts = [p.strip() for p in line.split(",")]
+      if len(parts) < 9:
+        continue
+      try:
+        sm.append(float(parts[1]))
+        smax = max(smax, float(parts[2]))
+      except ValueError:
+        continue
+      for name, val in zip(names, parts[5:9]):
+        if val.lower().startswith("active"):
+          reasons.add(name)
+    if not sm:
+      return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def make_graph(args):
+  from ceregraphs_gb300 import generators
+  t0 = time.perf_counter()
+  a = generators.rmat(args.scale, args.edgefactor, args.seed)
+  return a, time.perf_counter() - t0
+
+
+def workload_config(args, a, extra=None):
+  cfg = {"workload": f"rmat{args.scale}-e{args.edgefactor}-seed{args.seed}, "
+                     f"{args.roots} Graph500 roots (seed {args.root_seed}), one "
+                     f"{args.direction} search per root",
+         "scale": args.scale, "edgefactor": args.edgefactor, "n": a.n, "nnz": a.nnz,
+         "roots": args.roots, "root_seed": args.root_seed, "direction": args.direction,
+         "l2": f"inputs larger than L2: CSR {(a.nnz * 4 + (a.n + 1) * 8) / 1e6:.0f} MB",
+         "parallelism": f"replicas{args.gpus}"}
+  if extra:
+    cfg.update(extra)
+  return cfg
+
+
+# --------------------------------------------------------------------------
+# reference arm / CPU baseline: scipy breadth_first_order on A^T
+# --------------------------------------------------------------------------
+_REF = {}
+
+
+def _ref_init(indptr, indices, n):
+  from scipy import sparse
+  A = sparse.csr_matrix((np.ones(len(indices), dtype=np.int8), indices, indptr), shape=(n, n))
+  _REF["At"] = A.transpose().tocsr()
+
+
+def _ref_search(root):
+  from scipy.sparse.csgraph import breadth_first_order
+  t0 = time.perf_counter()
+  order, _ = breadth_first_order(_REF["At"], int(root), directed=True, return_predecessors=True)
+  dt = time.perf_counter() - t0
+  visited = np.zeros(_REF["At"].shape[0], dtype=bool)
+  visited[order] = True
+  return int(root), dt, visited
+
+
+def cpu_reference_sample(a, roots, seconds_budget, processes):
+  """Runs scipy BFS over roots (one per worker), stopping when the budget is
+  spent; returns per-root (root, seconds, m)."""
+  import multiprocessing as mp
+  from ceregraphs_gb300.graph500 import EdgeCounter
+  counter = EdgeCounter(a)
+  _ref_init(a.in_off, a.in_idx, a.n)
+  out = []
+  t_start = time.perf_counter()
+  if processes <= 1:
+    for r in roots:
+      root, dt, visited = _ref_search(r)
+      out.append((root, dt, counter.m(visited)))
+      if time.perf_counter() - t_start > seconds_budget:
+        break
+    return out, 1
+  ctx = mp.get_context("fork")
+  with ctx.Pool(processes) as pool:
+    i = 0
+    while i < len(roots):
+      batch = roots[i:i + processes]
+      for root, dt, visited in pool.map(_ref_search, batch):
+        out.append((root, dt, counter.m(visited)))
+      i += len(batch)
+      if time.perf_counter() - t_start > seconds_budget:
+        break
+  return out, processes
+
+
+def run_reference(args):
+  rank, world, _ = dist_env()
+  if rank != 0:
+    return 0
+  from ceregraphs_gb300.bfs_timing import harmonic_mean
+  from ceregraphs_gb300.graph500 import pick_sources
+  a, _ = make_graph(args)
+  roots = pick_sources(a, args.roots, args.root_seed)
+  cores = os.cpu_count() or 1
+  # warmup: one search per worker (bounded)
+  per_step = max(1, min(len(roots), cores))
+  cpu_reference_sample(a, roots[:per_step], 1e9, min(cores, per_step))
+  t0 = time.perf_counter()
+  samples = []
+  for s in range(args.steps):
+    sel = [roots[(s * per_step + j) % len(roots)] for j in range(per_step)]
+    res, used = cpu_reference_sample(a, sel, 1e9, min(cores, per_step))
+    samples.extend(res)
+  wall = time.perf_counter() - t0
+  g = [m / dt / 1e9 for (_, dt, m) in samples]
+  value = harmonic_mean(g)
+  line = {"metric": "GTEPS (harmonic mean over roots), per-root search",
+          "value": value, "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
+          "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+          "data": "synthetic (RMAT, reference generator recipe)", "impl": "reference",
+          "config": workload_config(args, a, {"parallelism": "host cores"}),
+          "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": min(cores, per_step),
+                           "kind": "reference",
+                           "sample": f"{len(samples)} searches ({per_step} per step, one per "
+                                     "core) of scipy.sparse.csgraph.breadth_first_order on A^T, "
+                                     "the call of run_graph500.py:383-395"},
+          "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                  "d2h_bytes_per_step": 0},
+          "aggregate_gteps_all_cores": sum(m for (_, _, m) in samples) / wall / 1e9}
+  print(json.dumps(line), flush=True)
+  return 0
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def run_ours(args):
+  import torch
+  rank, world, local = dist_env()
+  torch.cuda.set_device(local)
+  dist = None
+  if world > 1:
+    import torch.distributed as dist
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+  from ceregraphs_gb300 import _lib
+  from ceregraphs_gb300.bfs_timing import harmonic_mean
+  from ceregraphs_gb300.engine import Graph, PinnedBuffer
+  from ceregraphs_gb300.graph500 import EdgeCounter, pick_sources
+
+  a, gen_s = make_graph(args)
+  roots_all = pick_sources(a, args.roots, args.root_seed)
+  roots = roots_all  # every replica runs the full root set (weak scaling)
+  counter = EdgeCounter(a)
+  deg = np.diff(a.in_off if a.symmetric else a.out_off)
+
+  t0 = time.perf_counter()
+  g = Graph(a)
+  torch.cuda.synchronize()
+  construct_s = time.perf_counter() - t0
+  dirmap = {"auto": _lib.CG_DIR_AUTO, "topdown": _lib.CG_DIR_TOPDOWN,
+            "bottomup": _lib.CG_DIR_BOTTOMUP, "tau": _lib.CG_DIR_TAU}
+  g.set_options(direction=dirmap[args.direction])
+
+  n = a.n
+  k = len(roots)
+  d_lv = torch.empty((k, n), dtype=torch.int32, device="cuda")
+  d_pa = torch.empty((k, n), dtype=torch.int32, device="cuda")
+  torch.cuda.synchronize()
+  stream = torch.cuda.ExternalStream(g.stream)
+
+  # m per root (device count, checked once against the host rule below)
+  for i, r in enumerate(roots):
+    g.bfs_device(r, d_lv[i], d_pa[i])
+  st = g.last_stats()
+  if st["status"] != 0:
+    raise RuntimeError(f"search failed: {st}")
+  m = g.count_edges(d_lv, k)
+  lv_host = d_lv.cpu().numpy()
+  m_host = np.array([counter.m(lv_host[i] >= 0) for i in range(k)])
+  assert np.array_equal(m, m_host), "device and host edge counts differ"
+  nnz_vis = np.array([int(deg[lv_host[i] >= 0].sum()) for i in range(k)])
+  alg_bytes = 4 * nnz_vis + 8 * (n + 1) + 8 * n   # B_1 per search
+
+  def one_step(ev):
+    for i, r in enumerate(roots):
+      ev[i][0].record(stream)
+      g.bfs_device(r, d_lv[i], d_pa[i])
+      ev[i][1].record(stream)
+
+  events = [[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+            for _ in range(k)]
+  for _ in range(max(args.warmup, 3)):
+    one_step(events)
+  torch.cuda.synchronize()
+
+  sampler = ClockSampler(local)
+  sampler.start()
+  time.sleep(0.3)
+  if dist is not None:
+    dist.barrier()
+  torch.cuda.synchronize()
+  per_root_ms = np.zeros(k)
+  t_step0 = time.perf_counter()
+  for _ in range(args.steps):
+    one_step(events)
+    torch.cuda.synchronize()
+    per_root_ms += np.array([events[i][0].elapsed_time(events[i][1]) for i in range(k)])
+  torch.cuda.synchronize()
+  if dist is not None:
+    dist.barrier()
+  wall = time.perf_counter() - t_step0
+  per_root_ms /= args.steps
+  st = g.last_stats()
+  if st["status"] != 0:
+    raise RuntimeError(f"search failed: {st}")
+
+  # e2e: C ABI with host (page-locked) parent buffers, host clock per search
+  pin = PinnedBuffer(n)
+  e2e_s = np.zeros(k)
+  for i, r in enumerate(roots[:4]):  # warm
+    g.bfs(r, None, pin.array, want_levels=False)
+  for _ in range(args.steps):
+    for i, r in enumerate(roots):
+      t0 = time.perf_counter()
+      _, _, st2 = g.bfs(r, None, pin.array, want_levels=False)
+      e2e_s[i] += time.perf_counter() - t0
+  e2e_s /= args.steps
+  clocks = sampler.stop()
+
+  gteps_dev = m / (per_root_ms * 1e-3) / 1e9
+  gteps_e2e = m / e2e_s / 1e9
+  value = harmonic_mean(gteps_dev)
+  e2e_value = harmonic_mean(gteps_e2e)
+  step_ms = wall / args.steps * 1e3
+  if dist is not None:
+    t = torch.tensor([step_ms], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms = float(t.item())
+  peak, peak_kind = peaks()
+  achieved = float(alg_bytes.sum() / (per_root_ms.sum() * 1e-3) / 1e9)
+  traffic = NCU_TRAFFIC_BYTES
+  line = {
+      "metric": "GTEPS (harmonic mean over 64 roots), per-root direction-optimizing search",
+      "value": value * world, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+      "warmup": max(args.warmup, 3), "ms_per_step": step_ms, "higher_is_better": True,
+      "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+      "data": "synthetic (RMAT, the reference generator's recipe, bit-identical)",
+      "config": workload_config(args, a, {"construction_s": round(construct_s, 4),
+                                          "generation_s": round(gen_s, 2)}),
+      "e2e": {"value": e2e_value * world, "unit": "GTEPS", "h2d_bytes_per_step": 8 * k,
+              "d2h_bytes_per_step": 4 * n * k,
+              "note": "cg_bfs: launch + all rounds + parents copied to page-locked host memory"},
+      "gpu_launches": k * args.steps,
+      "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                   "frac": achieved / peak, "traffic": traffic,
+                   "kernel": "bfs_persistent",
+                   "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
+                   "measured" else "fallback 6.8 TB/s",
+                   "algorithmic_bytes": "4*nnz_visited + 8*(n+1) + 8*n per search"},
+      "per_root": {"ms_median": float(np.median(per_root_ms)),
+                   "ms_min": float(per_root_ms.min()), "ms_max": float(per_root_ms.max()),
+                   "gteps_min": float(gteps_dev.min()), "gteps_max": float(gteps_dev.max()),
+                   "e2e_ms_median": float(np.median(e2e_s) * 1e3),
+                   "rounds": st["rounds"], "pull_rounds_last": st["pull_rounds"]},
+  }
+  if clocks:
+    line["clocks"] = clocks
+  if rank == 0 and not args.no_cpu_baseline:
+    res, used = cpu_reference_sample(a, roots, args.cpu_seconds, 1)
+    g_cpu = [mm / dt / 1e9 for (_, dt, mm) in res]
+    line["cpu_baseline"] = {
+        "value": harmonic_mean(g_cpu), "unit": "GTEPS", "cores": 1, "kind": "reference",
+        "sample": f"{len(res)} of the {k} roots, scipy breadth_first_order on A^T "
+                  f"(run_graph500.py:383-395), single-threaded, {os.cpu_count()} host cores seen"}
+  g.close()
+  if rank == 0:
+    print(json.dumps(line), flush=True)
+  if dist is not None:
+    dist.destroy_process_group()
+  return 0
+
+
+def main():
+  args = parse()
+  if args.impl == "reference":
+    return run_reference(args)
+  return run_ours(args)
+
+
+if __name__ == "__main__":
+  sys.exit(main())

@@ -1,0 +1,187 @@
+// Internal definitions shared by the engine's translation units.
+//
+// Layout in HBM of one resident graph (cg_graph):
+//   in_off  int64[n+1], in_idx  int32[nnz]   CSR of A (row r = sources of edges c -> r)
+//   out_off int64[n+1], out_idx int32[nnz]   CSC of A (column c = targets of c);
+//                                             aliases of in_* when A is symmetric
+// Per-root search state (allocated once per handle, reused by every search):
+//   vis, cur, nxt  uint32[words]  packed bitmaps (visited, frontier, next frontier);
+//                                 the reference's visited_bitmap / x_bitmap / y_bitmap
+//                                 (bool_pe.csl) over all n vertices instead of per PE
+//   queue[2]       int32[n]       push-round frontier queues; light vertices fill
+//                                 from the front, medium ones from the back
+//   heavy[2]       int32[hcap]    vertices whose adjacency is split over the grid
+//   ctl            BfsCtl         per-round counters, grid-wait state, status
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ceregraphs.h"
+
+namespace cg {
+
+// Degree classes of a push-round frontier vertex.
+constexpr int kLightMax = 64;     // <= this: 32 vertices share one warp (edge-balanced)
+constexpr int kMediumMax = 4096;  // <= this: one warp per vertex; above: whole grid
+
+constexpr int kRing = 4;          // per-round record ring (rounds L .. L+3)
+
+// Statistics of frontier F_k (the vertices at level k) and the queue holding it.
+struct RoundRec {
+  unsigned long long nf;       // |F_k|
+  unsigned long long mf;       // sum of out-degrees over F_k
+  unsigned long long visdeg;   // sum of degrees over F_k (for unexplored-edge count)
+  unsigned int nlight;         // queue front
+  unsigned int nmedium;        // queue back
+  unsigned int nheavy;         // heavy list
+  unsigned int work;           // dynamic work counter used while F_k is expanded
+  unsigned long long pad[4];
+};
+
+struct GridWait {
+  unsigned int count;
+  unsigned int gen;
+  unsigned int pad[30];
+};
+
+struct BfsCtl {
+  GridWait wait;               // own 128-byte line
+  int status;
+  int rounds;
+  unsigned long long visited;
+  int pull_rounds;
+  int switches;
+  int pad[26];
+  RoundRec rec[kRing];
+};
+
+struct BfsParams {
+  int64_t n, nnz, words;
+  const int64_t *__restrict__ in_off;
+  const int32_t *__restrict__ in_idx;
+  const int64_t *__restrict__ out_off;
+  const int32_t *__restrict__ out_idx;
+  uint32_t *vis, *cur, *nxt;
+  int32_t *queue0, *queue1;
+  int32_t *heavy0, *heavy1;
+  int32_t *levels, *parents;
+  BfsCtl *ctl;
+  cg_stats *stats;
+  int64_t root;
+  int direction;
+  float alpha, beta;
+  int64_t tau;
+  int level_cap;
+  long long timeout_ns;
+  int unmatched_wait;
+};
+
+}  // namespace cg
+
+struct cg_graph {
+  int device = 0;
+  int num_sms = 0;
+  int64_t n = 0, nnz = 0;
+  bool symmetric = false;
+  int64_t *in_off = nullptr;
+  int32_t *in_idx = nullptr;
+  int64_t *out_off = nullptr;
+  int32_t *out_idx = nullptr;
+  cudaStream_t stream = nullptr;
+  cg_options opt{};
+  // per-root search state
+  int64_t words = 0;
+  uint32_t *bitmaps = nullptr;  // vis | cur | nxt, 3 * words
+  int32_t *queue = nullptr;     // 2 * n
+  int32_t *heavy = nullptr;     // 2 * hcap
+  int64_t hcap = 0;
+  cg::BfsCtl *ctl = nullptr;
+  cg_stats *d_stats = nullptr;
+  int32_t *tmp_levels = nullptr;   // host-output searches land here first
+  int32_t *tmp_parents = nullptr;
+  int bfs_grid = 0, bfs_block = 0;
+  // multi-source state (allocated on first use)
+  int ms_lane_words = 0;
+  uint64_t *ms_bits = nullptr;     // vis | cur | nxt, 3 * n * lane_words
+  int32_t *ms_levels = nullptr;    // host-output batches land here first
+  int32_t *ms_parents = nullptr;
+  int64_t ms_out_cap = 0;          // elements of ms_levels / ms_parents
+  void *ms_ctl = nullptr;
+  int ms_grid = 0, ms_block = 0;
+  int64_t device_bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace cg {
+// Records a CUDA error for cg_last_error_string and returns CG_ERR_CUDA.
+int cuda_fail(cudaError_t e, const char *what);
+int bfs_prepare(cg_graph *g);
+int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems);
+void msbfs_release(cg_graph *g);
+}  // namespace cg
+
+#define CG_CUDA(call)                                    \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return cg::cuda_fail(_e, #call); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+namespace cg {
+
+__device__ __forceinline__ long long global_ns() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide wait for a cooperative launch (all blocks co-resident).  Every
+// wait is bounded: after `timeout_ns` (or once another block has flagged an
+// error) the block records CG_ERR_TIMEOUT and the caller leaves its loop, so
+// a wait that can never complete ends the kernel instead of spinning.
+// `extra` > 0 makes the wait expect that many arrivals that never come (the
+// test hook behind cg_options.test_unmatched_wait).
+__device__ __forceinline__ bool grid_wait(GridWait *w, int *status, long long timeout_ns,
+                                          unsigned extra = 0) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned *vgen = &w->gen;
+    unsigned g = *vgen;
+    __threadfence();
+    unsigned target = gridDim.x + extra;
+    unsigned arrived = atomicAdd(&w->count, 1u) + 1u;
+    if (arrived == target) {
+      w->count = 0;
+      __threadfence();
+      atomicAdd(&w->gen, 1u);
+    } else {
+      long long t0 = global_ns();
+      unsigned spins = 0;
+      while (*vgen == g) {
+        if ((++spins & 63u) == 0) {
+          if (*(volatile int *)status != 0 || global_ns() - t0 > timeout_ns) {
+            atomicCAS(status, 0, (int)CG_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ int warp_id_global() {
+  return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+}
+__device__ __forceinline__ int lane_id() { return (int)(threadIdx.x & 31); }
+
+}  // namespace cg

@@ -1,0 +1,165 @@
+/*
+ * ceregraphs.h -- C ABI of the GB300 (sm_103a) BFS engine.
+ *
+ * This is the drop-in boundary for CereGraphs' on-device BFS.  The reference
+ * exposes its kernel through the Cerebras SdkRuntime symbol table of
+ * bfs/implementation/src/layout_bool.csl:84-122 (buffers x_bitmap,
+ * parent_local_buf, rounds_completed, mat_* ... and the function f_spmv_iter),
+ * driven by bfs/scripts/run_graph500.py:248-375 through memcpy_h2d / launch /
+ * memcpy_d2h.  Each entry point below names the reference step it replaces.
+ *
+ * Matrix convention (as in the reference, docs/GRAPH500_BENCHMARK.md:126-128):
+ * A[r, c] != 0 means an edge c -> r.  A search from `root` follows out-edges.
+ *   in_off / in_idx   = CSR of A: row r lists the sources c of edges c -> r,
+ *                       ascending (the reference's A_csr, run_graph500.py:165-168)
+ *   out_off / out_idx = CSC of A: column c lists the targets of c, ascending
+ *                       (the reference's A_csc, run_graph500.py:185-187);
+ *                       pass NULL for a symmetric A.
+ *
+ * Outputs are int32 per vertex: level (-1 = unreached, root = 0) and parent
+ * (-1 = unreached, parent[root] = root), the reference's readback convention
+ * (device_io.py:157-205, run_graph500.py:377-380).  The parent of v is the
+ * lowest-numbered in-neighbour one level closer to the root (the rule of
+ * bfs/README.md:208-224), so results do not depend on scheduling.
+ *
+ * All functions return 0 (CG_OK) or a positive cg_status code.  A handle is
+ * used by one host thread at a time; each handle owns one CUDA stream.
+ */
+#ifndef CEREGRAPHS_H
+#define CEREGRAPHS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cg_status {
+  CG_OK = 0,
+  CG_ERR_INVALID_ARG = 1,   /* bad pointer, size or root (run_graph500.py:111 asserts) */
+  CG_ERR_OUT_OF_MEMORY = 2, /* device allocation failed */
+  CG_ERR_CUDA = 3,          /* a CUDA runtime call failed; see cg_last_error_string */
+  CG_ERR_LEVEL_CAP = 4,     /* the search ran more rounds than the cap allows */
+  CG_ERR_TIMEOUT = 5,       /* a device-side wait ran out; the context stays usable */
+  CG_ERR_NOT_SUPPORTED = 6, /* e.g. cooperative launch unavailable */
+  CG_ERR_ADMISSION = 7      /* refused: the request does not fit the HBM budget */
+} cg_status;
+
+typedef struct cg_graph cg_graph;
+
+/* Direction policy of the per-root search. */
+enum {
+  CG_DIR_AUTO = 0,          /* direction-optimizing (Beamer): alpha / beta switches */
+  CG_DIR_TOPDOWN = 1,       /* push only: what run_graph500.py runs (tau = 0xFFFFFFFF) */
+  CG_DIR_BOTTOMUP = 2,      /* pull from round 1 on (round 0 is always push) */
+  CG_DIR_TAU = 3            /* one-way switch when nf > tau_switch_count
+                               (bool_pe.csl:1078-1088, run_bfs.py:239-243) */
+};
+
+/* Graph flags for cg_graph_create. */
+enum {
+  CG_GRAPH_DEVICE_PTRS = 1, /* the CSR/CSC arrays are device pointers (copied) */
+  CG_GRAPH_SYMMETRIC = 2    /* A == A^T: out_off/out_idx are ignored */
+};
+
+typedef struct cg_options {
+  int32_t direction;        /* CG_DIR_* */
+  float alpha;              /* push->pull when frontier edges > unexplored edges / alpha */
+  float beta;               /* pull->push when frontier vertices < n / beta (and shrinking) */
+  int64_t tau_switch_count; /* CG_DIR_TAU threshold; the reference uses round(0.15 n) */
+  int32_t block_size;       /* threads per block of the persistent kernel (multiple of 32) */
+  int32_t blocks_per_sm;    /* 0 = as many as fit */
+  int32_t level_cap;        /* stop with CG_ERR_LEVEL_CAP after this many rounds (0 = n + 1) */
+  int32_t wait_timeout_ms;  /* bound on each grid-wide wait (default 1000) */
+  int32_t lane_words;       /* multi-source: 1 = 64 lanes, 2 = 128 lanes per pass */
+  int32_t test_unmatched_wait; /* test hook: 1 makes the first grid-wide wait wait for an
+                                  arrival that never comes, so it must time out */
+} cg_options;
+
+#define CG_HISTORY 64
+
+typedef struct cg_stats {
+  int32_t status;           /* cg_status of the device run */
+  int32_t rounds;           /* rounds_completed: max level + 1 (bool_pe.csl:989) */
+  int64_t visited;          /* vertices reached, root included */
+  int32_t pull_rounds;      /* rounds run bottom-up */
+  int32_t switches;         /* direction changes */
+  float device_ms;          /* device time of the search (CUDA events), 0 if not timed */
+  int32_t history_len;      /* min(rounds, CG_HISTORY) */
+  int64_t nf_history[CG_HISTORY];      /* new vertices found per round (nf_history) */
+  int32_t direction_history[CG_HISTORY]; /* 0 push, 1 pull (direction_history) */
+} cg_stats;
+
+/* ---- library ---------------------------------------------------------- */
+int cg_version(void);
+const char *cg_strerror(int status);
+/* Text of the last CUDA error seen by this thread (empty if none). */
+const char *cg_last_error_string(void);
+void cg_default_options(cg_options *opt);
+
+/* ---- Kernel 1: construction ------------------------------------------
+ * Replaces the matrix upload of run_graph500.py:284-315 (seven memcpy_h2d
+ * of mat_rows/col_idx/col_loc/col_len/local_nnz*) and the 2-D partition of
+ * preprocess_bool.py:29-229: the whole CSR (and CSC if directed) becomes
+ * device-resident once and serves every later search. */
+int cg_graph_create(int64_t n, int64_t nnz, const int64_t *in_off, const int32_t *in_idx,
+                    const int64_t *out_off, const int32_t *out_idx, int32_t flags,
+                    cg_graph **out);
+int cg_graph_destroy(cg_graph *g);
+int cg_graph_set_options(cg_graph *g, const cg_options *opt);
+int cg_graph_get_options(const cg_graph *g, cg_options *opt);
+/* n, nnz, symmetric flag and device bytes held by the handle (graph + state). */
+int cg_graph_info(const cg_graph *g, int64_t *n, int64_t *nnz, int32_t *symmetric,
+                  int64_t *device_bytes);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order work on it. */
+void *cg_graph_stream(const cg_graph *g);
+
+/* ---- Kernel 2: one search --------------------------------------------
+ * Replaces single_source_seed_pe + memcpy_h2d(x_bitmap) (device_io.py:119-148,
+ * run_graph500.py:325-335), launch("f_spmv_iter") (run_graph500.py:339,
+ * bool_pe.csl:742-744 and the round loop :673-1161) and memcpy_d2h of
+ * parent_local_buf (run_graph500.py:347-358) plus extract_parent_result
+ * (device_io.py:160-178).  Host output buffers of n int32 each; either may be
+ * NULL.  Blocks until the outputs are in host memory. */
+int cg_bfs(cg_graph *g, int64_t root, int32_t *levels, int32_t *parents, cg_stats *stats);
+
+/* Same search with device output pointers (n int32 each, both required),
+ * enqueued on the handle's stream; returns without waiting.  Read the
+ * outcome with cg_graph_last_stats. */
+int cg_bfs_device(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents);
+
+/* Waits for the handle's stream, then reports the last search's device
+ * statistics (rounds_completed, nf_history, direction_history, status). */
+int cg_graph_last_stats(cg_graph *g, cg_stats *stats);
+
+/* ---- Kernel 2, batched: k searches in one pass ------------------------
+ * Multi-source BFS: roots packed as bit lanes per vertex (64 or 128 lanes a
+ * pass, cg_options.lane_words), a boolean SpMM per round.  No reference
+ * counterpart as one call: it replaces run_graph500.py:321-440's per-root
+ * loop of seed/launch/readback.  Outputs are root-major: levels[i * n + v].
+ * Host buffers of k * n int32 each (either may be NULL); blocks. */
+int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int32_t *parents,
+             cg_stats *stats);
+/* Device-pointer form (both outputs required), enqueued on the handle's
+ * stream.  d_roots is a HOST array of k roots. */
+int cg_msbfs_device(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels,
+                    int32_t *d_parents);
+
+/* ---- metric ------------------------------------------------------------
+ * Graph500 edges traversed per search, compute_m_and_gteps
+ * (bfs_timing.py:379-398): symmetric A counts (r, c) with r visited and
+ * c <= r; directed A counts entries whose source c is visited.  d_levels are
+ * k device arrays of n int32 laid out root-major; m_out receives k counts. */
+int cg_count_edges(cg_graph *g, const int32_t *d_levels, int32_t k, int64_t *m_out);
+
+/* ---- host memory ----------------------------------------------------------
+ * Page-locked host buffers, so that the parent/level readback of cg_bfs runs
+ * at full link speed (the reference's d2h of parent_local_buf,
+ * run_graph500.py:347-358, is part of each search's time). */
+int cg_host_alloc(void **ptr, int64_t bytes);
+int cg_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CEREGRAPHS_H */

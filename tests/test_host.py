@@ -1,0 +1,138 @@
+"""Host-side logic of the package (no GPU): generators, root sampling, the
+edge-count metric, readback conventions, CSR/CSC preparation, the ABI."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from golden_data import arrays, csr_from, golden, sha
+from ceregraphs_gb300 import bfs_timing, device_io, generators, graph500, preprocess
+
+G = golden()
+ARR = arrays()
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("key", ["s8_e16_seed0", "s10_e16_seed0", "s12_e4_seed0",
+                                 "s14_e16_seed3"])
+def test_product_rmat_is_bit_identical_to_reference(key):
+  g = G["graphs"][key]
+  a = generators.rmat(g["scale"], g["edgefactor"], g["seed"])
+  assert a.symmetric and a.n == g["n"] and a.nnz == g["nnz"]
+  assert sha(a.in_off.astype(np.int64)) == g["indptr_sha"]
+  assert sha(a.in_idx.astype(np.int32)) == g["indices_sha"]
+
+
+def test_product_rmat_chunked_draws_match_unchunked():
+  u1, v1 = generators.rmat_edge_endpoints(9, 8, 4, chunk=1 << 30)
+  u2, v2 = generators.rmat_edge_endpoints(9, 8, 4, chunk=777)
+  assert np.array_equal(u1, u2) and np.array_equal(v1, v2)
+
+
+def test_pick_sources_matches_reference():
+  for key, roots in G["pick_sources"].items():
+    if key.startswith("dir600"):
+      A = csr_from(ARR["dir600_indptr"], ARR["dir600_indices"], 600)
+      a = preprocess.preprocess(A)
+      k, seed = 6, 7
+    else:
+      gk, rest = key.rsplit("_k", 1)
+      k, seed = (int(x) for x in rest.split("_seed"))
+      g = G["graphs"][gk]
+      a = generators.rmat(g["scale"], g["edgefactor"], g["seed"])
+    assert graph500.pick_sources(a, k, seed) == roots, key
+
+
+def test_harmonic_mean_matches_reference():
+  for case in G["harmonic_mean"]:
+    vals = [float(v) for v in case["values"]]
+    got, want = bfs_timing.harmonic_mean(vals), float(case["hm"])
+    assert (np.isnan(got) and np.isnan(want)) or got == want
+
+
+def test_edge_counter_matches_reference_m():
+  g = G["graphs"]["s12_e16_seed0"]
+  a = generators.rmat(g["scale"], g["edgefactor"], g["seed"])
+  ec = graph500.EdgeCounter(a)
+  for rec in G["searches"]["s12_e16_seed0"]:
+    lv = ARR[f"s12_e16_seed0_r{rec['source']}_levels"]
+    assert ec.m(lv >= 0) == rec["m"]
+    assert bfs_timing.compute_m(a.scipy_csr(), lv >= 0, True) == rec["m"]
+  D = csr_from(ARR["dir600_indptr"], ARR["dir600_indices"], 600)
+  d = preprocess.preprocess(D)
+  assert not d.symmetric
+  ec = graph500.EdgeCounter(d)
+  for rec in G["searches"]["dir600"]:
+    lv = ARR[f"dir600_r{rec['source']}_levels"]
+    assert ec.m(lv >= 0) == rec["m"]
+
+
+def test_device_io_conventions():
+  raw = np.array([5, 0xFFFFFFFF, 2, 0xFFFFFFFF], dtype=np.uint32)
+  p = device_io.extract_parent_result(4, raw)
+  assert p.tolist() == [5, -1, 2, -1]
+  assert device_io.extract_parent_result(4, raw.view(np.int32)).tolist() == [5, -1, 2, -1]
+  assert device_io.derive_visited_from_parent(4, p, 1).tolist() == [True, True, True, False]
+  with pytest.raises(ValueError):
+    device_io.check_root(4, 4)
+
+
+def test_preprocess_directed_keeps_both_orientations():
+  D = csr_from(ARR["dir600_indptr"], ARR["dir600_indices"], 600)
+  a = preprocess.preprocess(D)
+  C = D.tocsc()
+  C.sort_indices()
+  assert np.array_equal(a.out_off, C.indptr) and np.array_equal(a.out_idx, C.indices)
+  for off, idx in ((a.in_off, a.in_idx), (a.out_off, a.out_idx)):
+    for v in range(0, 600, 13):
+      row = idx[off[v]:off[v + 1]]
+      assert np.all(np.diff(row) > 0)
+
+
+def test_er_and_grid_generators():
+  e = generators.er_directed(10, 8, 4)
+  assert not e.symmetric and e.n == 1024
+  A = e.scipy_csr()
+  assert A.diagonal().sum() == 0 and A.nnz == e.nnz <= 1024 * 8
+  g = generators.grid2d(5)
+  assert g.symmetric and g.n == 25 and g.nnz == 2 * 2 * 5 * 4
+  deg = np.diff(g.in_off)
+  assert deg[0] == 2 and deg[6] == 4
+
+
+def _declared_functions():
+  text = open(os.path.join(ROOT, "include", "ceregraphs.h"), encoding="utf-8").read()
+  text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+  return sorted(set(re.findall(r"\b(cg_\w+)\s*\(", text)))
+
+
+def test_abi_library_exports_every_declared_symbol(built_lib):
+  from ceregraphs_gb300 import _lib
+  declared = _declared_functions()
+  assert declared, "no declarations parsed"
+  for name in declared:
+    assert name in _lib.SIGNATURES, f"{name} has no binding"
+    assert hasattr(built_lib, name), f"{name} not exported"
+  assert set(_lib.SIGNATURES) == set(declared)
+
+
+def test_abi_calls_that_need_no_gpu(built_lib):
+  from ceregraphs_gb300 import _lib
+  assert built_lib.cg_version() >= 10000
+  assert built_lib.cg_strerror(_lib.CG_ERR_TIMEOUT).decode().startswith("device-side wait")
+  opt = _lib.default_options()
+  assert opt.direction == _lib.CG_DIR_AUTO and opt.lane_words == 1
+  # argument checks return before any CUDA call
+  h = ctypes.c_void_p()
+  assert built_lib.cg_graph_create(0, 0, None, None, None, None, 0, ctypes.byref(h)) == \
+      _lib.CG_ERR_INVALID_ARG
+  off = np.array([0, 1, 1], dtype=np.int64)
+  bad = np.array([7], dtype=np.int32)  # index out of range
+  assert built_lib.cg_graph_create(2, 1, off.ctypes.data_as(ctypes.c_void_p),
+                                   bad.ctypes.data_as(ctypes.c_void_p), None, None,
+                                   _lib.CG_GRAPH_SYMMETRIC, ctypes.byref(h)) == \
+      _lib.CG_ERR_INVALID_ARG
+  assert built_lib.cg_bfs(None, 0, None, None, None) == _lib.CG_ERR_INVALID_ARG
+  assert built_lib.cg_graph_destroy(None) == _lib.CG_ERR_INVALID_ARG
