@@ -36,7 +36,8 @@ class CgOptions(ctypes.Structure):
               ("beta", ctypes.c_float), ("tau_switch_count", ctypes.c_int64),
               ("block_size", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
               ("level_cap", ctypes.c_int32), ("wait_timeout_ms", ctypes.c_int32),
-              ("lane_words", ctypes.c_int32), ("test_unmatched_wait", ctypes.c_int32)]
+              ("lane_words", ctypes.c_int32), ("ms_alpha", ctypes.c_float),
+              ("test_unmatched_wait", ctypes.c_int32)]
 
   def as_dict(self):
     return {k: getattr(self, k) for k, _ in self._fields_}
@@ -91,6 +92,10 @@ SIGNATURES = {
     "cg_count_edges": ([_P, _P, ctypes.c_int32, _I64P], ctypes.c_int),
     "cg_host_alloc": ([ctypes.POINTER(_P), ctypes.c_int64], ctypes.c_int),
     "cg_host_free": ([_P], ctypes.c_int),
+    "cg_capture_begin": ([_P], ctypes.c_int),
+    "cg_capture_end": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
+    "cg_exec_launch": ([_P], ctypes.c_int),
+    "cg_exec_destroy": ([_P], ctypes.c_int),
 }
 
 _lib = None

@@ -103,6 +103,7 @@ void cg_default_options(cg_options *opt) {
   opt->level_cap = 0;
   opt->wait_timeout_ms = 1000;
   opt->lane_words = 1;
+  opt->ms_alpha = 4.f;
   opt->test_unmatched_wait = 0;
 }
 
@@ -176,7 +177,8 @@ int cg_graph_set_options(cg_graph *g, const cg_options *opt) {
   if (opt->block_size < 0 || (opt->block_size % 32) != 0 || opt->block_size > 512)
     return CG_ERR_INVALID_ARG;
   if (opt->lane_words != 1 && opt->lane_words != 2) return CG_ERR_INVALID_ARG;
-  if (opt->alpha < 0 || opt->beta < 0 || opt->level_cap < 0 || opt->wait_timeout_ms < 0)
+  if (opt->alpha < 0 || opt->beta < 0 || opt->ms_alpha < 0 || opt->level_cap < 0 ||
+      opt->wait_timeout_ms < 0)
     return CG_ERR_INVALID_ARG;
   g->opt = *opt;
   if (g->opt.tau_switch_count < 0) g->opt.tau_switch_count = (int64_t)(0.15 * (double)g->n + 0.5);
@@ -306,6 +308,53 @@ int cg_host_alloc(void **ptr, int64_t bytes) {
 int cg_host_free(void *ptr) {
   if (!ptr) return CG_ERR_INVALID_ARG;
   CG_CUDA(cudaFreeHost(ptr));
+  return CG_OK;
+}
+
+struct cg_exec {
+  cg_graph *g;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+};
+
+int cg_capture_begin(cg_graph *g) {
+  if (!g) return CG_ERR_INVALID_ARG;
+  CG_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeRelaxed));
+  return CG_OK;
+}
+
+int cg_capture_end(cg_graph *g, cg_exec **out) {
+  if (!g || !out) return CG_ERR_INVALID_ARG;
+  *out = nullptr;
+  cudaGraph_t graph = nullptr;
+  CG_CUDA(cudaStreamEndCapture(g->stream, &graph));
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  cg_exec *x = new (std::nothrow) cg_exec{g, graph, exec};
+  if (!x) {
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    return CG_ERR_OUT_OF_MEMORY;
+  }
+  *out = x;
+  return CG_OK;
+}
+
+int cg_exec_launch(cg_exec *x) {
+  if (!x) return CG_ERR_INVALID_ARG;
+  CG_CUDA(cudaGraphLaunch(x->exec, x->g->stream));
+  return CG_OK;
+}
+
+int cg_exec_destroy(cg_exec *x) {
+  if (!x) return CG_ERR_INVALID_ARG;
+  cudaGraphExecDestroy(x->exec);
+  cudaGraphDestroy(x->graph);
+  delete x;
   return CG_OK;
 }
 

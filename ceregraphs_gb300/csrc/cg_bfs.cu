@@ -522,9 +522,17 @@ int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents)
   p.unmatched_wait = g->opt.test_unmatched_wait;
   // every launch starts from a clean control block (round records, wait counter)
   CG_CUDA(cudaMemsetAsync(g->ctl, 0, sizeof(BfsCtl), g->stream));
-  void *args[] = {&p};
-  CG_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_persistent, dim3(g->bfs_grid),
-                                      dim3(g->bfs_block), args, 0, g->stream));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g->bfs_grid);
+  cfg.blockDim = dim3(g->bfs_block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = g->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // all blocks co-resident (grid waits)
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CG_CUDA(cudaLaunchKernelEx(&cfg, bfs_persistent, p));
   return CG_OK;
 }
 

@@ -53,6 +53,27 @@ class PinnedBuffer:
       pass
 
 
+class Exec:
+  """An instantiated CUDA graph of captured searches (cg_exec)."""
+
+  def __init__(self, handle):
+    self._x = handle
+
+  def launch(self):
+    check(_lib.load().cg_exec_launch(self._x), "cg_exec_launch")
+
+  def close(self):
+    if self._x is not None and self._x.value:
+      _lib.load().cg_exec_destroy(self._x)
+    self._x = None
+
+  def __del__(self):
+    try:
+      self.close()
+    except Exception:
+      pass
+
+
 class Graph:
   """A graph resident in HBM (in-lists, plus out-lists when directed)."""
 
@@ -177,6 +198,19 @@ class Graph:
     pp = d_parents if isinstance(d_parents, int) else d_parents.data_ptr()
     check(_lib.load().cg_msbfs_device(self._h, _ptr(roots), len(roots), ctypes.c_void_p(lp),
                                       ctypes.c_void_p(pp)), "cg_msbfs_device")
+
+  def capture(self, body):
+    """Record the searches that ``body()`` enqueues on this handle (the
+    ``*_device`` calls) into one CUDA graph; returns an Exec to replay it."""
+    lib = _lib.load()
+    check(lib.cg_capture_begin(self._h), "cg_capture_begin")
+    try:
+      body()
+    finally:
+      x = ctypes.c_void_p()
+      rc = lib.cg_capture_end(self._h, ctypes.byref(x))
+    check(rc, "cg_capture_end")
+    return Exec(x)
 
   def count_edges(self, d_levels, k=1):
     """Graph500 m for k searches whose levels are on the device (k x n)."""

@@ -72,6 +72,7 @@ typedef struct cg_options {
   int32_t level_cap;        /* stop with CG_ERR_LEVEL_CAP after this many rounds (0 = n + 1) */
   int32_t wait_timeout_ms;  /* bound on each grid-wide wait (default 1000) */
   int32_t lane_words;       /* multi-source: 1 = 64 lanes, 2 = 128 lanes per pass */
+  float ms_alpha;           /* multi-source: pull when frontier edges > nnz / ms_alpha */
   int32_t test_unmatched_wait; /* test hook: 1 makes the first grid-wide wait wait for an
                                   arrival that never comes, so it must time out */
 } cg_options;
@@ -151,6 +152,17 @@ int cg_msbfs_device(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_lev
  * c <= r; directed A counts entries whose source c is visited.  d_levels are
  * k device arrays of n int32 laid out root-major; m_out receives k counts. */
 int cg_count_edges(cg_graph *g, const int32_t *d_levels, int32_t k, int64_t *m_out);
+
+/* ---- CUDA graphs -----------------------------------------------------------
+ * Capture the searches enqueued on a handle's stream (cg_bfs_device,
+ * cg_msbfs_device) between begin and end into one executable CUDA graph, and
+ * replay it with one launch.  The captured searches keep the roots and
+ * output pointers they were given. */
+typedef struct cg_exec cg_exec;
+int cg_capture_begin(cg_graph *g);
+int cg_capture_end(cg_graph *g, cg_exec **out);
+int cg_exec_launch(cg_exec *e);
+int cg_exec_destroy(cg_exec *e);
 
 /* ---- host memory ----------------------------------------------------------
  * Page-locked host buffers, so that the parent/level readback of cg_bfs runs
