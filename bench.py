@@ -52,6 +52,8 @@ def parse():
   ap.add_argument("--cpu-seconds", type=float, default=15.0,
                   help="bound on the CPU-baseline sample")
   ap.add_argument("--no-cpu-baseline", action="store_true")
+  ap.add_argument("--no-batched", action="store_true",
+                  help="skip the multi-source (bit-lane) measurement")
   return ap.parse_args()
 
 
@@ -326,6 +328,44 @@ def run_ours(args):
       _, _, st2 = g.bfs(r, None, pin.array, want_levels=False)
       e2e_s[i] += time.perf_counter() - t0
   e2e_s /= args.steps
+
+  # batched: the same roots as bit lanes (64 or 128 per pass), one CUDA graph
+  # per step; every lane is checked against the per-root outputs
+  batched = None
+  if not args.no_batched:
+    ref_lv, ref_pa = d_lv.clone(), d_pa.clone()
+    g.set_options(lane_words=1 if k <= 64 else 2)
+    g.msbfs_device(roots, d_lv, d_pa)
+    g.last_stats()
+    exe = g.capture(lambda: g.msbfs_device(roots, d_lv, d_pa))
+    for _ in range(max(args.warmup, 3)):
+      exe.launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+      exe.launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / args.steps
+    stb = g.last_stats()
+    same = bool(torch.equal(ref_lv, d_lv) and torch.equal(ref_pa, d_pa))
+    exe.close()
+    pin_lv, pin_pa = PinnedBuffer((k, n)), PinnedBuffer((k, n))
+    g.msbfs(roots, pin_lv.array, pin_pa.array)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+      g.msbfs(roots, pin_lv.array, pin_pa.array)
+    batch_e2e_s = (time.perf_counter() - t0) / args.steps
+    batched_gteps = float(m.sum() / (batch_ms * 1e-3) / 1e9)
+    hm_per_root = harmonic_mean(m / (per_root_ms * 1e-3) / 1e9)
+    batched = {"gteps": batched_gteps, "ms": batch_ms,
+               "vs_per_root_harmonic_mean": batched_gteps / hm_per_root,
+               "e2e_gteps": float(m.sum() / batch_e2e_s / 1e9), "e2e_ms": batch_e2e_s * 1e3,
+               "lanes": 64 * (1 if k <= 64 else 2), "rounds": stb["rounds"],
+               "pull_rounds": stb["pull_rounds"], "bit_exact_vs_per_root": same,
+               "launch": "one cooperative kernel per 64/128 roots, replayed as a CUDA graph"}
+    del ref_lv, ref_pa
   clocks = sampler.stop()
 
   gteps_dev = m / (per_root_ms * 1e-3) / 1e9
@@ -364,6 +404,8 @@ def run_ours(args):
                    "e2e_ms_median": float(np.median(e2e_s) * 1e3),
                    "rounds": st["rounds"], "pull_rounds_last": st["pull_rounds"]},
   }
+  if batched:
+    line["batched"] = batched
   if clocks:
     line["clocks"] = clocks
   if rank == 0 and not args.no_cpu_baseline:
