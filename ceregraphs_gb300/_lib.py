@@ -92,6 +92,12 @@ SIGNATURES = {
     "cg_count_edges": ([_P, _P, ctypes.c_int32, _I64P], ctypes.c_int),
     "cg_host_alloc": ([ctypes.POINTER(_P), ctypes.c_int64], ctypes.c_int),
     "cg_host_free": ([_P], ctypes.c_int),
+    "cg_rmat_edges": ([ctypes.c_int32, ctypes.c_int64, _P, _P, _P, _P, _P], ctypes.c_int),
+    "cg_uniform_bits": ([_P, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int32, _P, _P],
+                        ctypes.c_int),
+    "cg_graph_from_edges": ([ctypes.c_int64, ctypes.c_int64, _P, _P, ctypes.c_int32,
+                             ctypes.POINTER(_P)], ctypes.c_int),
+    "cg_graph_export": ([_P, _P, _P, _P, _P], ctypes.c_int),
     "cg_capture_begin": ([_P], ctypes.c_int),
     "cg_capture_end": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
     "cg_exec_launch": ([_P], ctypes.c_int),

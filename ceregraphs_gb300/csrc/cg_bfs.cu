@@ -35,6 +35,8 @@ namespace cg {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kPush = 0, kPull = 1;
 constexpr int kBfsBlock = 512;
+// In-degree above which a pull-round in-list is scanned by a whole warp.
+constexpr int kPullLight = 32;
 
 struct Acc {
   unsigned long long nf = 0, mf = 0, visdeg = 0;
@@ -208,12 +210,42 @@ __device__ void pull_round(const BfsParams &p, int L, Acc &acc) {
     if (active) {
       s = __ldg(p.in_off + v);
       e = __ldg(p.in_off + v + 1);
+    }
+    const bool heavy = active && (e - s) > kPullLight;
+    if (active && !heavy) {
       for (int64_t i = s; i < e; ++i) {
         const int32_t u = __ldg(p.in_idx + i);
         if ((p.cur[(uint32_t)u >> 5] >> (u & 31)) & 1u) {
           p.parents[v] = u;
           p.levels[v] = L + 1;
           found = true;
+          break;
+        }
+      }
+    }
+    // long in-lists: the whole warp scans one at a time, 32 sources per step;
+    // the lowest lane with a frontier source holds the smallest one
+    unsigned hm = __ballot_sync(kFull, heavy);
+    while (hm) {
+      const int j = __ffs(hm) - 1;
+      hm &= hm - 1;
+      const int64_t sj = __shfl_sync(kFull, s, j), ej = __shfl_sync(kFull, e, j);
+      const int64_t vj = w * 32 + j;
+      for (int64_t base = sj; base < ej; base += 32) {
+        const int64_t i = base + lane;
+        int32_t u = 0;
+        bool hit = false;
+        if (i < ej) {
+          u = __ldg(p.in_idx + i);
+          hit = (p.cur[(uint32_t)u >> 5] >> (u & 31)) & 1u;
+        }
+        const unsigned who = __ballot_sync(kFull, hit);
+        if (who) {
+          if (lane == __ffs(who) - 1) {
+            p.parents[vj] = u;
+            p.levels[vj] = L + 1;
+          }
+          if (lane == j) found = true;
           break;
         }
       }

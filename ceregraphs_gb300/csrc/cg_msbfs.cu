@@ -38,8 +38,12 @@ struct MsRound {
   unsigned long long visits;  // lane discoveries
   unsigned long long mf;      // sum of out-degrees over the frontier vertices
   unsigned int nlight, nmedium, nheavy, work;
-  unsigned long long pad[3];
+  unsigned long long lanes[2];  // lanes whose frontier is non-empty
+  unsigned long long pad;
 };
+
+// In-degree above which a vertex's in-list is scanned by a whole warp.
+constexpr int kPullLight = 32;
 
 struct MsCtl {
   GridWait wait;
@@ -169,6 +173,7 @@ __device__ __forceinline__ void write_lanes(const MsParams &p, int64_t v, const 
 
 struct MsAcc {
   unsigned long long nf = 0, visits = 0, mf = 0;
+  unsigned long long lanes[2] = {0ull, 0ull};
 };
 
 // Appends claimed vertices to the next frontier's queue (all lanes call).
@@ -215,13 +220,26 @@ __device__ __forceinline__ unsigned long long ms_warp_sum(unsigned long long x) 
 
 __device__ void ms_flush(MsAcc &acc, MsRound *Rn) {
   __shared__ unsigned long long s_red[3][kMsBlock / 32];
+  __shared__ unsigned long long s_lanes[2];
   const int lane = lane_id(), wib = threadIdx.x >> 5;
+  if (threadIdx.x < 2) s_lanes[threadIdx.x] = 0ull;
   unsigned long long a = ms_warp_sum(acc.nf), b = ms_warp_sum(acc.visits),
                      c = ms_warp_sum(acc.mf);
+  unsigned long long l0 = acc.lanes[0], l1 = acc.lanes[1];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l0 |= __shfl_xor_sync(kMsFull, l0, o);
+    l1 |= __shfl_xor_sync(kMsFull, l1, o);
+  }
   if (lane == 0) {
     s_red[0][wib] = a;
     s_red[1][wib] = b;
     s_red[2][wib] = c;
+  }
+  __syncthreads();
+  if (lane == 0) {
+    if (l0) atomicOr(&s_lanes[0], l0);
+    if (l1) atomicOr(&s_lanes[1], l1);
   }
   __syncthreads();
   if (wib == 0) {
@@ -233,45 +251,135 @@ __device__ void ms_flush(MsAcc &acc, MsRound *Rn) {
       if (a) atomicAdd(&Rn->nf, a);
       if (b) atomicAdd(&Rn->visits, b);
       if (c) atomicAdd(&Rn->mf, c);
+      if (s_lanes[0]) atomicOr(&Rn->lanes[0], s_lanes[0]);
+      if (s_lanes[1]) atomicOr(&Rn->lanes[1], s_lanes[1]);
     }
   }
   __syncthreads();
   acc = MsAcc();
 }
 
-// Pull round over every vertex with unvisited lanes.
+template <int W>
+__device__ __forceinline__ void acc_lanes(MsAcc &acc, const Mask<W> &m) {
+#pragma unroll
+  for (int i = 0; i < W; ++i) acc.lanes[i] |= m.w[i];
+}
+
+// Warp-cooperative scan of vertex v's ascending in-list (all 32 lanes call
+// with the same v and want): 32 sources per step; for each lane bit found in
+// a step, the lowest warp lane holding it -- the smallest source -- is the
+// parent.  Stops once every wanted bit is found.  Returns the found bits.
+template <int W>
+__device__ Mask<W> warp_scan_in_list(const MsParams &p, int64_t v, const Mask<W> &want,
+                                     const uint64_t *cur, int level) {
+  const int lane = lane_id();
+  Mask<W> got = Mask<W>::zero();
+  const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+  for (int64_t base = s; base < e; base += 32) {
+    const int64_t i = base + lane;
+    Mask<W> f = Mask<W>::zero();
+    int32_t u = 0;
+    if (i < e) {
+      u = __ldg(p.in_idx + i);
+      f = (ld_mask<W>(cur, u) & want).andnot(got);
+    }
+    Mask<W> F = f;
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) F.w[j] |= __shfl_xor_sync(kMsFull, F.w[j], o);
+    if (F.any()) {
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        uint64_t bits = F.w[j];
+        while (bits) {
+          const int b = __ffsll((long long)bits) - 1;
+          bits &= bits - 1;
+          const unsigned who = __ballot_sync(kMsFull, (f.w[j] >> b) & 1ull);
+          if (lane == __ffs(who) - 1) {
+            const int64_t at = (int64_t)(j * 64 + b) * p.n + v;
+            p.levels[at] = level;
+            p.parents[at] = u;
+          }
+        }
+      }
+      got = got | F;
+      if (got == want) break;
+    }
+  }
+  return got;
+}
+
+// Thread-level scan of the same kind, for short in-lists.
+template <int W>
+__device__ __forceinline__ Mask<W> thread_scan_in_list(const MsParams &p, int64_t v,
+                                                       const Mask<W> &want,
+                                                       const uint64_t *cur, int level) {
+  Mask<W> got = Mask<W>::zero();
+  const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+  for (int64_t i = s; i < e; ++i) {
+    const int32_t u = __ldg(p.in_idx + i);
+    const Mask<W> f = (ld_mask<W>(cur, u) & want).andnot(got);
+    if (f.any()) {
+      write_lanes<W>(p, v, f, u, level);
+      got = got | f;
+      if (got == want) break;
+    }
+  }
+  return got;
+}
+
+// Scans a warp's 32 vertices: short lists one per thread, long ones by the
+// whole warp in turn.  want must be zero for vertices that need no scan.
+template <int W>
+__device__ __forceinline__ Mask<W> scan_group(const MsParams &p, int64_t v, const Mask<W> &want,
+                                              const uint64_t *cur, int level) {
+  const bool need = want.any();
+  const int64_t deg = need ? (__ldg(p.in_off + v + 1) - __ldg(p.in_off + v)) : 0;
+  const bool heavy = need && deg > kPullLight;
+  Mask<W> got = Mask<W>::zero();
+  if (need && !heavy) got = thread_scan_in_list<W>(p, v, want, cur, level);
+  unsigned hm = __ballot_sync(kMsFull, heavy);
+  while (hm) {
+    const int j = __ffs(hm) - 1;
+    hm &= hm - 1;
+    const int64_t vj = __shfl_sync(kMsFull, v, j);
+    Mask<W> wj;
+#pragma unroll
+    for (int i = 0; i < W; ++i) wj.w[i] = __shfl_sync(kMsFull, want.w[i], j);
+    const Mask<W> gj = warp_scan_in_list<W>(p, vj, wj, cur, level);
+    if (lane_id() == j) got = gj;
+  }
+  return got;
+}
+
+// Pull round over every vertex with unvisited lanes whose frontier is not
+// empty (`active`: lanes whose search has ended cannot be found any more).
 template <int W>
 __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
-                        const Mask<W> &all, MsRound *Rn, MsAcc &acc) {
+                        const Mask<W> &active, MsRound *Rn, MsAcc &acc) {
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
        base < p.n; base += nthreads) {
     const int64_t v = base + lane_id();
+    Mask<W> want = Mask<W>::zero();
+    Mask<W> seen = Mask<W>::zero();
+    if (v < p.n) {
+      seen = ld_mask<W>(p.vis, v);
+      want = active.andnot(seen);
+    }
+    if (!__ballot_sync(kMsFull, want.any())) continue;
+    const Mask<W> got = scan_group<W>(p, v, want, cur, L + 1);
     bool claimed = false;
     int64_t deg = 0;
-    if (v < p.n) {
-      const Mask<W> want = all.andnot(ld_mask<W>(p.vis, v));
-      if (want.any()) {
-        Mask<W> got = Mask<W>::zero();
-        const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
-        for (int64_t i = s; i < e; ++i) {
-          const int32_t u = __ldg(p.in_idx + i);
-          const Mask<W> f = (ld_mask<W>(cur, u) & want).andnot(got);
-          if (f.any()) {
-            write_lanes<W>(p, v, f, u, L + 1);
-            got = got | f;
-            if (got == want) break;
-          }
-        }
-        if (got.any()) {
-          st_mask<W>(nxt, v, got);
-          st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | got);
-          claimed = true;
-          acc.visits += (unsigned long long)got.popc();
-          deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
-        }
-      }
+    if (got.any()) {
+      st_mask<W>(nxt, v, got);
+      st_mask<W>(p.vis, v, seen | got);
+      claimed = true;
+      acc.visits += (unsigned long long)got.popc();
+      acc_lanes<W>(acc, got);
+      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
     }
     ms_enqueue(p, claimed, (int32_t)v, deg, next_parity, Rn, acc);
   }
@@ -402,7 +510,6 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
 template <int W>
 __device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, const uint64_t *nxt,
                            const MsRound *Rn, MsAcc &acc) {
-  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
   const int32_t *q = next_parity ? p.queue1 : p.queue0;
@@ -411,27 +518,25 @@ __device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, const 
   const int64_t nm = *(volatile unsigned *)&Rn->nmedium;
   const int64_t nh = *(volatile unsigned *)&Rn->nheavy;
   const int64_t total = nl + nm + nh;
-  for (int64_t j = gtid; j < total; j += nthreads) {
-    int32_t v;
-    if (j < nl)
-      v = q[j];
-    else if (j < nl + nm)
-      v = q[p.n - 1 - (j - nl)];
-    else
-      v = h[j - nl - nm];
-    const Mask<W> nw = ld_mask<W>(nxt, v);
-    st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
-    acc.visits += (unsigned long long)nw.popc();
-    Mask<W> pending = nw;
-    const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
-    for (int64_t i = s; i < e && pending.any(); ++i) {
-      const int32_t u = __ldg(p.in_idx + i);
-      const Mask<W> g = ld_mask<W>(cur, u) & pending;
-      if (g.any()) {
-        write_lanes<W>(p, v, g, u, L + 1);
-        pending = pending.andnot(g);
-      }
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total;
+       base += nthreads) {
+    const int64_t j = base + lane_id();
+    int64_t v = 0;
+    Mask<W> nw = Mask<W>::zero();
+    if (j < total) {
+      if (j < nl)
+        v = q[j];
+      else if (j < nl + nm)
+        v = q[p.n - 1 - (j - nl)];
+      else
+        v = h[j - nl - nm];
+      nw = ld_mask<W>(nxt, v);
+      st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
+      acc.visits += (unsigned long long)nw.popc();
+      acc_lanes<W>(acc, nw);
     }
+    // every lane of nw has a frontier source in v's in-list: the scan ends
+    scan_group<W>(p, v, nw, cur, L + 1);
   }
 }
 
@@ -441,7 +546,6 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
-  const Mask<W> all = lane_mask<W>(p.k);
   uint64_t *fr[3] = {p.fr0, p.fr1, p.fr2};
 
   // phase 0: clear the lane state
@@ -480,6 +584,11 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
         atomicAdd(&R0->nf, 1ull);
         atomicAdd(&R0->mf, (unsigned long long)deg);
       }
+      if (i == 0) {
+        const Mask<W> a0 = lane_mask<W>(p.k);
+        ctl->rec[0].lanes[0] = a0.w[0];
+        ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
+      }
     }
   }
   if (ok) ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
@@ -502,11 +611,15 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
       MsRound *Rz = &ctl->rec[(L + 3) % kRing];
       Rz->nf = Rz->visits = Rz->mf = 0;
       Rz->nlight = Rz->nmedium = Rz->nheavy = Rz->work = 0;
+      Rz->lanes[0] = Rz->lanes[1] = 0;
     }
     for (int64_t i = gtid; i < p.n * W; i += nthreads) old[i] = 0;
     for (int64_t w = gtid; w < p.words; w += nthreads) touched_next[w] = 0;
     if (dir == 1) {
-      ms_pull<W>(p, L, cur, nxt, all, Rn, acc);
+      Mask<W> active;
+#pragma unroll
+      for (int i = 0; i < W; ++i) active.w[i] = *(volatile unsigned long long *)&Rc->lanes[i];
+      ms_pull<W>(p, L, cur, nxt, active, Rn, acc);
       ms_flush(acc, Rn);
       if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
     } else {

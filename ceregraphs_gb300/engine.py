@@ -104,6 +104,27 @@ class Graph:
                               ctypes.byref(self._h)), "cg_graph_create")
     self.n, self.nnz, self.symmetric = a.n, a.nnz, a.symmetric
 
+  @classmethod
+  def from_handle(cls, handle):
+    """Adopt a cg_graph* made by another C-ABI call (e.g. cg_graph_from_edges)."""
+    g = cls.__new__(cls)
+    g._h = handle
+    info = g.info()
+    g.n, g.nnz, g.symmetric = info["n"], info["nnz"], info["symmetric"]
+    return g
+
+  def export(self) -> GraphArrays:
+    """Copy the resident CSR (and CSC when directed) back to host arrays."""
+    io = np.empty(self.n + 1, dtype=np.int64)
+    ii = np.empty(self.nnz, dtype=np.int32)
+    oo = oi = None
+    if not self.symmetric:
+      oo = np.empty(self.n + 1, dtype=np.int64)
+      oi = np.empty(self.nnz, dtype=np.int32)
+    check(_lib.load().cg_graph_export(self._h, _ptr(io), _ptr(ii), _ptr(oo), _ptr(oi)),
+          "cg_graph_export")
+    return GraphArrays(self.n, self.nnz, io, ii, oo, oi, self.symmetric)
+
   # -- lifecycle -----------------------------------------------------------
   def close(self):
     if self._h is not None and self._h.value:

@@ -164,6 +164,38 @@ int cg_capture_end(cg_graph *g, cg_exec **out);
 int cg_exec_launch(cg_exec *e);
 int cg_exec_destroy(cg_exec *e);
 
+/* ---- construction on the device -------------------------------------------
+ * Synthetic inputs and the edge-list -> CSR/CSC build run on the GPU.
+ *
+ * cg_rmat_edges: the R-MAT endpoints of datasets/gen_rmat.py:15-44, bit for
+ * bit: m = 2^scale * edgefactor pairs (u[e], v[e]) written to device arrays.
+ * gen_state = {state_hi, state_lo, inc_hi, inc_lo} of the PCG64 generator
+ * that np.random.default_rng(seed) starts from; thresholds = ceil(t * 2^53)
+ * for t = A, A+B, A+B+C.  `stream` is a cudaStream_t (NULL = default). */
+int cg_rmat_edges(int32_t scale, int64_t m, const uint64_t *gen_state,
+                  const uint64_t *thresholds, uint32_t *d_u, uint32_t *d_v, void *stream);
+/* floor(r * 2^bits) for the doubles r number first .. first+count-1 of the
+ * same generator stream (the directed Erdos-Renyi inputs). */
+int cg_uniform_bits(const uint64_t *gen_state, uint64_t first, int64_t count, int32_t bits,
+                    uint32_t *d_out, void *stream);
+
+/* Edge-list flags for cg_graph_from_edges. */
+enum {
+  CG_EDGES_SYMMETRIZE = 1,  /* store both directions (gen_rmat.py:34-36) */
+  CG_EDGES_DROP_LOOPS = 2   /* drop self-loops (gen_rmat.py:37-38) */
+};
+
+/* Kernel 1 from a device edge list src[e] -> dst[e] (entries A[dst, src]):
+ * sort, merge duplicates, build the CSR (and the CSC when not symmetrised)
+ * on the device and create the handle.  Replaces load_graph + tocsr +
+ * sorted_indices + tocsc (run_graph500.py:165-187) for generated inputs. */
+int cg_graph_from_edges(int64_t n, int64_t m, const uint32_t *d_src, const uint32_t *d_dst,
+                        int32_t flags, cg_graph **out);
+/* Copies the resident arrays to host buffers (any may be NULL): CSR offsets
+ * (n+1 int64) and indices (nnz int32), CSC likewise. */
+int cg_graph_export(const cg_graph *g, int64_t *in_off, int32_t *in_idx, int64_t *out_off,
+                    int32_t *out_idx);
+
 /* ---- host memory ----------------------------------------------------------
  * Page-locked host buffers, so that the parent/level readback of cg_bfs runs
  * at full link speed (the reference's d2h of parent_local_buf,

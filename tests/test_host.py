@@ -136,3 +136,12 @@ def test_abi_calls_that_need_no_gpu(built_lib):
       _lib.CG_ERR_INVALID_ARG
   assert built_lib.cg_bfs(None, 0, None, None, None) == _lib.CG_ERR_INVALID_ARG
   assert built_lib.cg_graph_destroy(None) == _lib.CG_ERR_INVALID_ARG
+
+
+def test_grid_csr_is_sorted_and_symmetric():
+  a = generators.grid2d(7)
+  A = a.scipy_csr()
+  assert (A != A.T).nnz == 0
+  for v in range(a.n):
+    row = a.in_idx[a.in_off[v]:a.in_off[v + 1]]
+    assert np.all(np.diff(row) > 0)
