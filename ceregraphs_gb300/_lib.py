@@ -49,14 +49,18 @@ class CgStats(ctypes.Structure):
               ("switches", ctypes.c_int32), ("device_ms", ctypes.c_float),
               ("history_len", ctypes.c_int32),
               ("nf_history", ctypes.c_int64 * CG_HISTORY),
-              ("direction_history", ctypes.c_int32 * CG_HISTORY)]
+              ("direction_history", ctypes.c_int32 * CG_HISTORY),
+              ("round_ns", ctypes.c_int64 * CG_HISTORY), ("setup_ns", ctypes.c_int64),
+              ("finish_ns", ctypes.c_int64)]
 
   def as_dict(self):
     h = self.history_len
     return {"status": self.status, "rounds": self.rounds, "visited": self.visited,
             "pull_rounds": self.pull_rounds, "switches": self.switches,
             "device_ms": self.device_ms, "nf_history": list(self.nf_history[:h]),
-            "direction_history": list(self.direction_history[:h])}
+            "direction_history": list(self.direction_history[:h]),
+            "round_ns": list(self.round_ns[:h]), "setup_ns": self.setup_ns,
+            "finish_ns": self.finish_ns}
 
 
 class CgError(RuntimeError):

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int32_t root = (int32_t)p.root;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  const long long t_start = leader ? global_ns() : 0;
 
   // ---- phase 0: start_spmv -- reset outputs and bitmaps, seed the root ----
   for (int64_t i = gtid; i < p.n; i += nthreads) {
@@ -399,9 +400,16 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
   unsigned long long prev_nf = 1, visited = 1;
   unsigned long long explored = (unsigned long long)(p.out_off[root + 1] - p.out_off[root]);
   Acc acc;
+  long long t_round = leader ? global_ns() : 0;
+  if (leader) p.stats->setup_ns = t_round - t_start;
   while (ok) {
     RoundRec *Rc = &ctl->rec[L % kRing];
     RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
+    if (leader && L > 0 && L - 1 < CG_HISTORY) {
+      const long long now = global_ns();
+      p.stats->round_ns[L - 1] = now - t_round;
+      t_round = now;
+    }
     if (dir == kPush)
       push_round(p, L, Rc, Rn, acc);
     else
@@ -444,6 +452,8 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
   }
   if (leader) {
     cg_stats *st = p.stats;
+    if (L > 0 && L - 1 < CG_HISTORY) st->round_ns[L - 1] = global_ns() - t_round;
+    st->finish_ns = 0;
     st->status = *(volatile int *)&ctl->status;
     st->rounds = L;
     st->visited = (int64_t)visited;

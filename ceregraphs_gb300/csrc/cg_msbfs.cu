@@ -546,6 +546,7 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  const long long t_start = leader ? global_ns() : 0;
   uint64_t *fr[3] = {p.fr0, p.fr1, p.fr2};
 
   // phase 0: clear the lane state
@@ -597,7 +598,14 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
   int L = 0, pull_rounds = 0, switches = 0;
   unsigned long long visited = (unsigned long long)p.k;
   MsAcc acc;
+  long long t_round = leader ? global_ns() : 0;
+  if (leader) p.stats->setup_ns = t_round - t_start;
   while (ok) {
+    if (leader && L > 0 && L - 1 < CG_HISTORY) {
+      const long long now = global_ns();
+      p.stats->round_ns[L - 1] = now - t_round;
+      t_round = now;
+    }
     const uint64_t *cur = fr[L % 3];
     uint64_t *nxt = fr[(L + 1) % 3];
     uint64_t *old = fr[(L + 2) % 3];
@@ -659,6 +667,11 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
     dir = next;
     ++L;
   }
+  long long t_finish = 0;
+  if (leader) {
+    t_finish = global_ns();
+    if (L > 0 && L - 1 < CG_HISTORY) p.stats->round_ns[L - 1] = t_finish - t_round;
+  }
   // unreached lanes: level and parent -1 (each (lane, vertex) is written once)
   if (ok) {
     for (int64_t v = gtid; v < p.n; v += nthreads) {
@@ -673,6 +686,7 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
   }
   if (leader) {
     cg_stats *st = p.stats;
+    st->finish_ns = global_ns() - t_finish;
     st->status = *(volatile int *)&ctl->status;
     st->rounds = L;
     st->visited = (int64_t)visited;

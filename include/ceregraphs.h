@@ -89,6 +89,10 @@ typedef struct cg_stats {
   int32_t history_len;      /* min(rounds, CG_HISTORY) */
   int64_t nf_history[CG_HISTORY];      /* new vertices found per round (nf_history) */
   int32_t direction_history[CG_HISTORY]; /* 0 push, 1 pull (direction_history) */
+  int64_t round_ns[CG_HISTORY]; /* device time of each round, grid waits included
+                                   (the reference's per-round ts_buf, bool_pe.csl:226-285) */
+  int64_t setup_ns;             /* state reset + seed, before round 0 */
+  int64_t finish_ns;            /* after the last round (output finishing) */
 } cg_stats;
 
 /* ---- library ---------------------------------------------------------- */
