@@ -102,6 +102,8 @@ SIGNATURES = {
     "cg_graph_from_edges": ([ctypes.c_int64, ctypes.c_int64, _P, _P, ctypes.c_int32,
                              ctypes.POINTER(_P)], ctypes.c_int),
     "cg_graph_export": ([_P, _P, _P, _P, _P], ctypes.c_int),
+    "cg_bfs_noalloc": ([ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, ctypes.c_int64, _P, _P,
+                        ctypes.POINTER(CgStats), _P], ctypes.c_int),
     "cg_capture_begin": ([_P], ctypes.c_int),
     "cg_capture_end": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
     "cg_exec_launch": ([_P], ctypes.c_int),

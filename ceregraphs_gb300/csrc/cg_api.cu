@@ -21,6 +21,8 @@ int cuda_fail(cudaError_t e, const char *what) {
   return CG_ERR_CUDA;
 }
 
+void set_error_text(const char *text) { snprintf(t_last_error, sizeof(t_last_error), "%s", text); }
+
 static void free_graph(cg_graph *g) {
   if (!g) return;
   int prev = 0;

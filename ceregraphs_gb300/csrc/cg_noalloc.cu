@@ -1,0 +1,154 @@
+// cg_bfs_noalloc: the per-root search for callers that cannot let the library
+// allocate device memory.
+//
+// Some callers own every byte of device memory they use and forbid anyone else
+// from calling cudaMalloc: runtimes that reserve the GPU up front in their own
+// pool (a JVM or Go service that binds this library over JNI/cgo and budgets
+// HBM itself), or real-time loops where an allocation's implicit device-wide
+// synchronisation would stall other work.  The handle API cannot serve them:
+// cg_graph_create allocates the graph copy and the search state.  This entry
+// point takes the caller's device CSR/CSC and output arrays as they are, and
+// keeps its search state (bitmaps, frontier queues, round records, statistics)
+// in one file-scope __device__ array of fixed size, which exists in every GPU
+// that loads the library until the process exits.  It calls no cudaMalloc,
+// cudaFree or allocating library routine; the search is the same persistent
+// kernel the handle API launches.
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+#include <mutex>
+
+#include "cg_internal.cuh"
+
+namespace cg {
+
+__global__ void bfs_persistent(BfsParams p);
+void set_error_text(const char *text);
+
+constexpr int64_t kNoAllocMaxVertices = CG_NOALLOC_MAX_VERTICES;
+constexpr int64_t kNoAllocMaxHeavy = CG_NOALLOC_MAX_HEAVY;
+constexpr int64_t kNoAllocWords = (kNoAllocMaxVertices + 31) / 32;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kOffCtl = 0;
+constexpr size_t kOffStats = align256(kOffCtl + sizeof(BfsCtl));
+constexpr size_t kOffBitmaps = align256(kOffStats + sizeof(cg_stats));
+constexpr size_t kOffQueue = align256(kOffBitmaps + sizeof(uint32_t) * 3 * kNoAllocWords);
+constexpr size_t kOffHeavy = align256(kOffQueue + sizeof(int32_t) * 2 * kNoAllocMaxVertices);
+constexpr size_t kScratchBytes = align256(kOffHeavy + sizeof(int32_t) * 2 * kNoAllocMaxHeavy);
+
+// The search state of every cg_bfs_noalloc call on this GPU (about 17 MiB).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_setup_mu;
+static void *g_scratch_addr[kMaxDevices] = {};
+static int g_grid[kMaxDevices] = {};
+
+// Once per device, with that device current: the device address of the
+// scratch array (host code cannot use the symbol itself) and the grid size.
+static int noalloc_setup(int dev, void **scratch, int *grid) {
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  if (!g_scratch_addr[dev]) {
+    void *addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    int sms = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bfs_persistent, 512, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+    g_grid[dev] = per_sm * sms;
+    g_scratch_addr[dev] = addr;
+  }
+  *scratch = g_scratch_addr[dev];
+  *grid = g_grid[dev];
+  return CG_OK;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
+                              const int32_t *d_in_idx, const int64_t *d_out_off,
+                              const int32_t *d_out_idx, int64_t root, int32_t *d_levels,
+                              int32_t *d_parents, cg_stats *stats, void *stream) {
+  if (n <= 0 || nnz < 0 || !d_in_off || (nnz > 0 && !d_in_idx) || !d_levels || !d_parents ||
+      root < 0 || root >= n || ((d_out_off == nullptr) != (d_out_idx == nullptr)))
+    return CG_ERR_INVALID_ARG;
+  const int64_t hcap = nnz / (kMediumMax + 1) + 1;
+  if (n > kNoAllocMaxVertices || (hcap < n ? hcap : n) > kNoAllocMaxHeavy) {
+    char msg[200];
+    snprintf(msg, sizeof(msg),
+             "cg_bfs_noalloc: graph exceeds the fixed scratch capacity (n = %lld > %lld "
+             "vertices, or more than %lld vertices of out-degree > %d)",
+             (long long)n, (long long)kNoAllocMaxVertices, (long long)kNoAllocMaxHeavy,
+             kMediumMax);
+    set_error_text(msg);
+    return CG_ERR_INVALID_ARG;
+  }
+  int dev = 0;
+  CG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return CG_ERR_NOT_SUPPORTED;
+  void *scratch = nullptr;
+  int grid = 0;
+  int rc = noalloc_setup(dev, &scratch, &grid);
+  if (rc) return rc;
+  unsigned char *base = static_cast<unsigned char *>(scratch);
+  const int64_t words = (n + 31) / 32;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  BfsParams p;
+  p.n = n;
+  p.nnz = nnz;
+  p.words = words;
+  p.in_off = d_in_off;
+  p.in_idx = d_in_idx;
+  p.out_off = d_out_off ? d_out_off : d_in_off;
+  p.out_idx = d_out_idx ? d_out_idx : d_in_idx;
+  uint32_t *bitmaps = reinterpret_cast<uint32_t *>(base + kOffBitmaps);
+  p.vis = bitmaps;
+  p.cur = bitmaps + words;
+  p.nxt = bitmaps + 2 * words;
+  int32_t *queue = reinterpret_cast<int32_t *>(base + kOffQueue);
+  p.queue0 = queue;
+  p.queue1 = queue + n;
+  int32_t *heavy = reinterpret_cast<int32_t *>(base + kOffHeavy);
+  p.heavy0 = heavy;
+  p.heavy1 = heavy + kNoAllocMaxHeavy;
+  p.levels = d_levels;
+  p.parents = d_parents;
+  p.ctl = reinterpret_cast<BfsCtl *>(base + kOffCtl);
+  p.stats = reinterpret_cast<cg_stats *>(base + kOffStats);
+  p.root = root;
+  p.direction = CG_DIR_AUTO;
+  p.alpha = 15.f;
+  p.beta = 18.f;
+  p.tau = (int64_t)(0.15 * (double)n + 0.5);
+  p.level_cap = (int)((n + 1) < 0x7fffffff ? n + 1 : 0x7fffffff);
+  p.timeout_ns = 1000ll * 1000000ll;
+  p.unmatched_wait = 0;
+  // The array keeps the previous call's contents: the round records and the
+  // grid-wait counter must start at zero (bitmaps and outputs are reset by the
+  // kernel itself).
+  CG_CUDA(cudaMemsetAsync(p.ctl, 0, sizeof(BfsCtl), st));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(512);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CG_CUDA(cudaLaunchKernelEx(&cfg, bfs_persistent, p));
+  if (stats) {
+    CG_CUDA(cudaMemcpyAsync(stats, p.stats, sizeof(cg_stats), cudaMemcpyDeviceToHost, st));
+    CG_CUDA(cudaStreamSynchronize(st));
+    return stats->status;
+  }
+  return CG_OK;
+}

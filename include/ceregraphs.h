@@ -98,7 +98,8 @@ typedef struct cg_stats {
 /* ---- library ---------------------------------------------------------- */
 int cg_version(void);
 const char *cg_strerror(int status);
-/* Text of the last CUDA error seen by this thread (empty if none). */
+/* Text of the last error seen by this thread: a CUDA error, or why a size was
+ * rejected (empty if none). */
 const char *cg_last_error_string(void);
 void cg_default_options(cg_options *opt);
 
@@ -199,6 +200,32 @@ int cg_graph_from_edges(int64_t n, int64_t m, const uint32_t *d_src, const uint3
  * (n+1 int64) and indices (nnz int32), CSC likewise. */
 int cg_graph_export(const cg_graph *g, int64_t *in_off, int32_t *in_idx, int64_t *out_off,
                     int32_t *out_idx);
+
+/* ---- one search without any library allocation --------------------------
+ * No counterpart in the reference.  For callers that cannot let this library
+ * allocate device memory: runtimes that reserve and budget the GPU's memory
+ * themselves (a JVM or Go server binding this ABI over JNI/cgo, a framework
+ * whose pool owns the device), and loops that cannot afford the device-wide
+ * synchronisation a cudaMalloc or cudaFree implies.  The caller passes its own
+ * device CSR (and CSC, or NULL for a symmetric A) and device outputs of n
+ * int32 each; the search state lives in one fixed __device__ array of this
+ * library (about 17 MiB, present on every GPU that loads the library until
+ * the process exits).  Nothing is allocated: no cudaMalloc, cudaFree or
+ * allocating library routine is called.
+ * Limits: n <= CG_NOALLOC_MAX_VERTICES and nnz / 4097 + 1 (the bound on
+ * vertices of out-degree > 4096) <= CG_NOALLOC_MAX_HEAVY; larger graphs are
+ * rejected with CG_ERR_INVALID_ARG and a message in cg_last_error_string.
+ * Every call on a GPU shares the array and it keeps the last call's contents:
+ * calls that overlap on that GPU (other streams or threads) race and give
+ * wrong results.  The first call on each device sets up the array's device
+ * address, so make it before any stream capture.  Direction policy: Beamer's
+ * alpha = 15, beta = 18.  With stats != NULL the call waits for `stream` and
+ * returns the search's status; with NULL it returns once the work is queued. */
+#define CG_NOALLOC_MAX_VERTICES (1 << 21)
+#define CG_NOALLOC_MAX_HEAVY (1 << 15)
+int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off, const int32_t *d_in_idx,
+                   const int64_t *d_out_off, const int32_t *d_out_idx, int64_t root,
+                   int32_t *d_levels, int32_t *d_parents, cg_stats *stats, void *stream);
 
 /* ---- host memory ----------------------------------------------------------
  * Page-locked host buffers, so that the parent/level readback of cg_bfs runs
