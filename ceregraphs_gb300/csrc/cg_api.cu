@@ -36,7 +36,7 @@ static void free_graph(cg_graph *g) {
   cudaFree(g->in_idx);
   cudaFree(g->bitmaps);
   cudaFree(g->queue);
-  cudaFree(g->heavy);
+  cudaFree(g->bigoff);
   cudaFree(g->ctl);
   cudaFree(g->d_stats);
   cudaFree(g->tmp_levels);
@@ -118,6 +118,8 @@ int cg_graph_create(int64_t n, int64_t nnz, const int64_t *in_off, const int32_t
   const bool sym = (flags & CG_GRAPH_SYMMETRIC) != 0;
   if (n <= 0 || n > 0x7fffffffLL || nnz < 0 || !in_off || (nnz > 0 && !in_idx))
     return CG_ERR_INVALID_ARG;
+  // frontier edge counts are 32-bit in the push rounds' chunking
+  if (nnz >= (1ll << 32) - (1ll << 16)) return CG_ERR_NOT_SUPPORTED;
   if (!sym && (!out_off || (nnz > 0 && !out_idx))) return CG_ERR_INVALID_ARG;
   if (!dev) {
     if (!valid_host_csr(n, nnz, in_off, in_idx)) return CG_ERR_INVALID_ARG;

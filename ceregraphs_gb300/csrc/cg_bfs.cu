@@ -1,19 +1,19 @@
 // Per-root direction-optimizing BFS: one persistent cooperative kernel that
-// runs every round of a search on the device.
+// runs every round of a search on the device, with one grid-wide wait per round.
 //
 // Reference mapping (bfs/implementation/src/bool_pe.csl):
 //   start_spmv (:673-729)          -> phase 0 of bfs_persistent (state reset, seed)
-//   compute_topdown (:865-887)     -> push_round: frontier queue, out-lists,
-//                                     atomicOr into the next-frontier bitmap
+//   compute_topdown (:865-887)     -> push_round_*: frontier queue (or bitmap),
+//                                     out-lists, atomicOr into the next frontier
 //   compute_bottomup (:899-921)    -> pull_round: unvisited vertices scan their
 //                                     ascending in-lists, stop at the first
 //                                     frontier source
 //   reduce_or + reduce_done        -> the shared bitmaps make the OR-reduce
-//     (:923-1004, collectives_2d     implicit; update_round applies
-//      pe.csl:319-349)                 visited |= next, frontier = next, and the
+//     (:923-1004, collectives_2d     implicit; the visited set is vis | F_L, and
+//      pe.csl:319-349)                 vis |= F_L is folded into round L's work;
 //                                     per-round counters give nf = popcount
 //   termination relay (:1003-1046)  -> every block reads nf from the round
-//                                     record after a grid-wide wait; nf == 0 ends
+//                                     record after the grid-wide wait; nf == 0 ends
 //   direction switch (:1078-1088)   -> next_direction(): Beamer's alpha/beta rule,
 //                                     or the reference's one-way tau rule
 //   reduce_select_any (:1145-1154)  -> not needed: every parent is final when it
@@ -21,11 +21,16 @@
 //
 // Parent rule: the lowest-numbered in-neighbour one level closer
 // (bfs/README.md:208-224).  A push round applies atomicMin over every
-// frontier source of a newly reached vertex (the visited bitmap is frozen
-// during the round, so all of them are seen); a pull round takes the first
-// frontier source of an ascending in-list, which is the minimum.  Parents
-// start at 0xFFFFFFFF, the reference's PARENT_NONE (device_io.py:157), which
-// reads back as -1 through int32 without a conversion pass.
+// frontier source of a newly reached vertex (the visited set is frozen during
+// the round, so all of them are seen); a pull round takes the first frontier
+// source of an ascending in-list, which is the minimum.  Parents start at
+// 0xFFFFFFFF, the reference's PARENT_NONE (device_io.py:157), which reads back
+// as -1 through int32 without a conversion pass.
+//
+// Bitmaps: vis holds the vertices of F_0 .. F_{L-1}, the frontier F_L is
+// fr[L % 3], the next frontier is written into fr[(L+1) % 3] and fr[(L+2) % 3]
+// (F_{L-1}) is cleared during round L.  "Visited" is tested as vis | F_L, so
+// merging F_L into vis during round L races with nothing.
 #include <cuda_runtime.h>
 
 #include "cg_internal.cuh"
@@ -35,43 +40,52 @@ namespace cg {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kPush = 0, kPull = 1;
 constexpr int kBfsBlock = 512;
-// In-degree above which a pull-round in-list is scanned by a whole warp.
-constexpr int kPullLight = 32;
+// Pull rounds: in-list entries each thread checks before the warp takes over.
+constexpr int kPullThreadScan = 8;
 
 struct Acc {
   unsigned long long nf = 0, mf = 0, visdeg = 0;
 };
 
-// Pushes the discoveries of one warp-wide step into the next frontier's queue
-// (light: front, medium: back, heavy: separate list).  All 32 lanes call it.
+// Appends the discoveries of one warp-wide step to the next frontier's queue:
+// light vertices at the front; big ones at the back, each with the prefix
+// offset of its edge list among the big vertices (one packed 64-bit atomic per
+// warp: count in the high word, edges in the low word).  All 32 lanes call.
 __device__ __forceinline__ void enqueue_claims(const BfsParams &p, bool claimed, int32_t v,
                                                int64_t deg, int next_parity, RoundRec *Rn,
                                                Acc &acc) {
   const int lane = lane_id();
-  unsigned any = __ballot_sync(kFull, claimed);
-  if (!any) return;
-  int cls = !claimed ? -1 : (deg <= kLightMax ? 0 : (deg <= kMediumMax ? 1 : 2));
+  if (!__ballot_sync(kFull, claimed)) return;
   int32_t *q = next_parity ? p.queue1 : p.queue0;
-  int32_t *h = next_parity ? p.heavy1 : p.heavy0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    unsigned m = __ballot_sync(kFull, cls == c);
-    if (!m) continue;
-    int leader = __ffs(m) - 1;
+  const bool light = claimed && deg <= kLightMax;
+  const bool big = claimed && deg > kLightMax;
+  const unsigned below = (1u << lane) - 1u;
+  const unsigned ml = __ballot_sync(kFull, light);
+  if (ml) {
+    const int leader = __ffs(ml) - 1;
     unsigned base = 0;
-    if (lane == leader) {
-      unsigned *ctr = c == 0 ? &Rn->nlight : (c == 1 ? &Rn->nmedium : &Rn->nheavy);
-      base = atomicAdd(ctr, (unsigned)__popc(m));
-    }
+    if (lane == leader) base = atomicAdd(&Rn->nlight, (unsigned)__popc(ml));
     base = __shfl_sync(kFull, base, leader);
-    if (cls == c) {
-      unsigned pos = base + __popc(m & ((1u << lane) - 1u));
-      if (c == 0)
-        q[pos] = v;
-      else if (c == 1)
-        q[p.n - 1 - (int64_t)pos] = v;
-      else
-        h[pos] = v;
+    if (light) q[base + __popc(ml & below)] = v;
+  }
+  const unsigned mb = __ballot_sync(kFull, big);
+  if (mb) {
+    const unsigned d = big ? (unsigned)deg : 0u;
+    unsigned incl = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const unsigned total = __shfl_sync(kFull, incl, 31);
+    unsigned long long old = 0;
+    if (lane == 0)
+      old = atomicAdd(&Rn->big, ((unsigned long long)__popc(mb) << 32) | total);
+    old = __shfl_sync(kFull, old, 0);
+    if (big) {
+      const unsigned idx = (unsigned)(old >> 32) + __popc(mb & below);
+      q[p.n - 1 - (int64_t)idx] = v;
+      (next_parity ? p.bigoff1 : p.bigoff0)[idx] = (unsigned)(old & 0xffffffffu) + incl - d;
     }
   }
   if (claimed) {
@@ -82,140 +96,192 @@ __device__ __forceinline__ void enqueue_claims(const BfsParams &p, bool claimed,
 }
 
 // Edge u -> v of a push round.  Returns true for the one thread that claims v.
-__device__ __forceinline__ bool relax_push(const BfsParams &p, int32_t u, int32_t v,
-                                           int next_level) {
+__device__ __forceinline__ bool relax_push(const BfsParams &p, const uint32_t *cur,
+                                           uint32_t *nxt, int32_t u, int32_t v, int next_level) {
   const uint32_t w = (uint32_t)v >> 5, bit = 1u << (v & 31);
-  if (p.vis[w] & bit) return false;
+  if ((p.vis[w] | cur[w]) & bit) return false;
   atomicMin(reinterpret_cast<unsigned *>(p.parents) + v, (unsigned)u);
-  if (p.nxt[w] & bit) return false;
-  unsigned old = atomicOr(p.nxt + w, bit);
+  if (nxt[w] & bit) return false;
+  const unsigned old = atomicOr(nxt + w, bit);
   if (old & bit) return false;
   p.levels[v] = next_level;
   return true;
 }
 
-__device__ __forceinline__ void push_step(const BfsParams &p, bool valid, int32_t u, int64_t e,
-                                          int L, int next_parity, RoundRec *Rn, Acc &acc) {
+__device__ __forceinline__ void push_step(const BfsParams &p, const uint32_t *cur, uint32_t *nxt,
+                                          bool valid, int32_t u, int64_t e, int L,
+                                          int next_parity, RoundRec *Rn, Acc &acc) {
   bool claimed = false;
   int32_t v = 0;
   int64_t deg = 0;
   if (valid) {
     v = __ldg(p.out_idx + e);
-    claimed = relax_push(p, u, v, L + 1);
+    claimed = relax_push(p, cur, nxt, u, v, L + 1);
     if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
   }
   enqueue_claims(p, claimed, v, deg, next_parity, Rn, acc);
 }
 
-// Expands frontier F_L (queue parity L & 1) top-down.
-__device__ void push_round(const BfsParams &p, int L, RoundRec *Rc, RoundRec *Rn, Acc &acc) {
+// Expands up to 32 frontier vertices (one per lane, u < 0 for none) with the
+// warp's combined edge list spread evenly over its lanes.
+__device__ __forceinline__ void gather_expand(const BfsParams &p, const uint32_t *cur,
+                                              uint32_t *nxt, int32_t u, int L, int next_parity,
+                                              RoundRec *Rn, Acc &acc, int32_t *s_u, int64_t *s_s,
+                                              int64_t *s_x) {
+  const int lane = lane_id();
+  int64_t s = 0, d = 0;
+  if (u >= 0) {
+    s = __ldg(p.out_off + u);
+    d = __ldg(p.out_off + u + 1) - s;
+  }
+  int64_t incl = d;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t t = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int64_t total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) return;
+  s_u[lane] = u;
+  s_s[lane] = s;
+  s_x[lane] = incl - d;
+  __syncwarp();
+  for (int64_t base = 0; base < total; base += 32) {
+    const int64_t t = base + lane;
+    const bool valid = t < total;
+    int32_t uu = 0;
+    int64_t e = 0;
+    if (valid) {
+      int lo = 0, hi = 31;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_x[mid] <= t)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      uu = s_u[lo];
+      e = s_s[lo] + (t - s_x[lo]);
+    }
+    push_step(p, cur, nxt, valid, uu, e, L, next_parity, Rn, acc);
+  }
+  __syncwarp();
+}
+
+// Expands frontier F_L from its queue (parity L & 1): edge-balanced chunks of
+// the big vertices' combined edge list, then the light vertices 32 to a warp.
+// Item i goes to warp i first; warps that finish take the rest from a counter.
+__device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
+                                 RoundRec *Rc, RoundRec *Rn, Acc &acc) {
   __shared__ int32_t s_u[kBfsBlock / 32][32];
   __shared__ int64_t s_s[kBfsBlock / 32][32];
-  __shared__ int32_t s_x[kBfsBlock / 32][32];
+  __shared__ int64_t s_x[kBfsBlock / 32][32];
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
-  const int gw = warp_id_global();
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int parity = L & 1, next_parity = parity ^ 1;
   const int32_t *q = parity ? p.queue1 : p.queue0;
-  const int32_t *h = parity ? p.heavy1 : p.heavy0;
+  const uint32_t *boff = parity ? p.bigoff1 : p.bigoff0;
 
-  // heavy vertices: each adjacency list is split over every warp of the grid
-  const unsigned nheavy = *(volatile unsigned *)&Rc->nheavy;
-  for (unsigned b = 0; b < nheavy; ++b) {
-    const int32_t u = h[b];
-    const int64_t s = __ldg(p.out_off + u), e = __ldg(p.out_off + u + 1);
-    for (int64_t base = s + (int64_t)gw * 32; base < e; base += (int64_t)nwarps * 32) {
-      const int64_t i = base + lane;
-      push_step(p, i < e, u, i, L, next_parity, Rn, acc);
-    }
-  }
-
-  // medium vertices (one warp each), then light vertices 32 to a warp with the
-  // warp's combined edge list spread evenly over its lanes
-  const unsigned nmed = *(volatile unsigned *)&Rc->nmedium;
+  const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
+  const unsigned nbig = (unsigned)(bigw >> 32);
+  const unsigned big_edges = (unsigned)(bigw & 0xffffffffu);
   const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
-  const unsigned nitems = nmed + (nlight + 31u) / 32u;
-  while (true) {
-    unsigned item = 0;
-    if (lane == 0) item = atomicAdd(&Rc->work, 1u);
-    item = __shfl_sync(kFull, item, 0);
-    if (item >= nitems) break;
-    if (item < nmed) {
-      const int32_t u = q[p.n - 1 - (int64_t)item];
-      const int64_t s = __ldg(p.out_off + u), e = __ldg(p.out_off + u + 1);
-      for (int64_t base = s; base < e; base += 32) {
-        const int64_t i = base + lane;
-        push_step(p, i < e, u, i, L, next_parity, Rn, acc);
+  const unsigned nchunks = (big_edges + kPushChunk - 1) / kPushChunk;
+  const unsigned nitems = nchunks + (nlight + 31u) / 32u;
+  unsigned item = (unsigned)warp_id_global();
+  while (item < nitems) {
+    if (item < nchunks) {
+      const unsigned x0 = item * kPushChunk;
+      const unsigned x1 = min(x0 + (unsigned)kPushChunk, big_edges);
+      // big vertex j holding edge position x0: the last j with boff[j] <= x0
+      unsigned lo = 0, hi = nbig - 1;
+      while (lo < hi) {
+        const unsigned mid = (lo + hi + 1) >> 1;
+        if (boff[mid] <= x0)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      unsigned j = lo;
+      int32_t vj = q[p.n - 1 - (int64_t)j];
+      int64_t sj = __ldg(p.out_off + vj);
+      unsigned oj = boff[j];
+      unsigned endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
+      for (unsigned base = x0; base < x1; base += 32) {
+        while (base >= endj) {  // the next big vertex (degrees exceed 32)
+          ++j;
+          vj = q[p.n - 1 - (int64_t)j];
+          sj = __ldg(p.out_off + vj);
+          oj = boff[j];
+          endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
+        }
+        const unsigned x = base + lane;
+        const bool valid = x < x1;
+        int32_t u = vj;
+        int64_t e = sj + (int64_t)(x - oj);
+        if (__ballot_sync(kFull, valid && x >= endj)) {  // lanes past vertex j's end
+          const int32_t vn = q[p.n - 1 - (int64_t)(j + 1)];
+          if (valid && x >= endj) {
+            u = vn;
+            e = __ldg(p.out_off + vn) + (int64_t)(x - endj);
+          }
+        }
+        push_step(p, cur, nxt, valid, u, e, L, next_parity, Rn, acc);
       }
     } else {
-      const unsigned idx = (item - nmed) * 32u + lane;
-      int32_t u = 0;
-      int64_t s = 0;
-      int d = 0;
-      if (idx < nlight) {
-        u = q[idx];
-        s = __ldg(p.out_off + u);
-        d = (int)(__ldg(p.out_off + u + 1) - s);
-      }
-      int incl = d;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const int total = __shfl_sync(kFull, incl, 31);
-      s_u[wib][lane] = u;
-      s_s[wib][lane] = s;
-      s_x[wib][lane] = incl - d;
-      __syncwarp();
-      for (int base = 0; base < total; base += 32) {
-        const int t = base + lane;
-        bool valid = t < total;
-        int32_t uu = 0;
-        int64_t e = 0;
-        if (valid) {
-          int lo = 0, hi = 31;
-          while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (s_x[wib][mid] <= t)
-              lo = mid;
-            else
-              hi = mid - 1;
-          }
-          uu = s_u[wib][lo];
-          e = s_s[wib][lo] + (t - s_x[wib][lo]);
-        }
-        push_step(p, valid, uu, e, L, next_parity, Rn, acc);
-      }
-      __syncwarp();
+      const unsigned idx = (item - nchunks) * 32u + lane;
+      gather_expand(p, cur, nxt, idx < nlight ? q[idx] : -1, L, next_parity, Rn, acc, s_u[wib],
+                    s_s[wib], s_x[wib]);
     }
+    unsigned nextitem = 0;
+    if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
+    item = __shfl_sync(kFull, nextitem, 0);
+  }
+}
+
+// Push round right after a pull round: the frontier is only in the bitmap, so
+// warps walk its words and expand the set bits 32 at a time.
+__device__ void push_round_bitmap(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
+                                  RoundRec *Rn, Acc &acc) {
+  __shared__ int32_t s_u[kBfsBlock / 32][32];
+  __shared__ int64_t s_s[kBfsBlock / 32][32];
+  __shared__ int64_t s_x[kBfsBlock / 32][32];
+  const int lane = lane_id();
+  const int wib = threadIdx.x >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int next_parity = (L + 1) & 1;
+  for (int64_t w = warp_id_global(); w < p.words; w += nwarps) {
+    const uint32_t bits = cur[w];
+    if (!bits) continue;
+    const int32_t u = ((bits >> lane) & 1u) ? (int32_t)(w * 32 + lane) : -1;
+    gather_expand(p, cur, nxt, u, L, next_parity, Rn, acc, s_u[wib], s_s[wib], s_x[wib]);
   }
 }
 
 // Bottom-up round: every unvisited vertex scans its ascending in-list and
-// stops at the first source in frontier F_L.  One warp owns one bitmap word,
-// so the next-frontier word is written whole, without atomics.
-__device__ void pull_round(const BfsParams &p, int L, Acc &acc) {
+// stops at the first source in F_L.  One warp owns one bitmap word (so the
+// next-frontier word is written whole, without atomics); each lane checks the
+// first kPullThreadScan sources itself, longer remainders are scanned by the
+// whole warp, 32 sources a step, one vertex at a time.
+__device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
+                           Acc &acc) {
   const int lane = lane_id();
-  const int gw = warp_id_global();
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = gw; w < p.words; w += nwarps) {
-    const uint32_t vw = p.vis[w];
+  for (int64_t w = warp_id_global(); w < p.words; w += nwarps) {
+    const uint32_t seen = p.vis[w] | cur[w];
     const int64_t v = w * 32 + lane;
-    const bool active = v < p.n && !((vw >> lane) & 1u);
+    const bool active = v < p.n && !((seen >> lane) & 1u);
     if (__ballot_sync(kFull, active) == 0) continue;
     bool found = false;
     int64_t s = 0, e = 0;
     if (active) {
       s = __ldg(p.in_off + v);
       e = __ldg(p.in_off + v + 1);
-    }
-    const bool heavy = active && (e - s) > kPullLight;
-    if (active && !heavy) {
-      for (int64_t i = s; i < e; ++i) {
+      const int64_t lim = min(e, s + (int64_t)kPullThreadScan);
+      for (int64_t i = s; i < lim; ++i) {
         const int32_t u = __ldg(p.in_idx + i);
-        if ((p.cur[(uint32_t)u >> 5] >> (u & 31)) & 1u) {
+        if ((cur[(uint32_t)u >> 5] >> (u & 31)) & 1u) {
           p.parents[v] = u;
           p.levels[v] = L + 1;
           found = true;
@@ -223,27 +289,25 @@ __device__ void pull_round(const BfsParams &p, int L, Acc &acc) {
         }
       }
     }
-    // long in-lists: the whole warp scans one at a time, 32 sources per step;
-    // the lowest lane with a frontier source holds the smallest one
-    unsigned hm = __ballot_sync(kFull, heavy);
-    while (hm) {
-      const int j = __ffs(hm) - 1;
-      hm &= hm - 1;
-      const int64_t sj = __shfl_sync(kFull, s, j), ej = __shfl_sync(kFull, e, j);
-      const int64_t vj = w * 32 + j;
+    unsigned rest = __ballot_sync(kFull, active && !found && e > s + kPullThreadScan);
+    while (rest) {
+      const int j = __ffs(rest) - 1;
+      rest &= rest - 1;
+      const int64_t sj = __shfl_sync(kFull, s, j) + kPullThreadScan;
+      const int64_t ej = __shfl_sync(kFull, e, j);
       for (int64_t base = sj; base < ej; base += 32) {
         const int64_t i = base + lane;
         int32_t u = 0;
         bool hit = false;
         if (i < ej) {
           u = __ldg(p.in_idx + i);
-          hit = (p.cur[(uint32_t)u >> 5] >> (u & 31)) & 1u;
+          hit = (cur[(uint32_t)u >> 5] >> (u & 31)) & 1u;
         }
         const unsigned who = __ballot_sync(kFull, hit);
         if (who) {
           if (lane == __ffs(who) - 1) {
-            p.parents[vj] = u;
-            p.levels[vj] = L + 1;
+            p.parents[w * 32 + j] = u;
+            p.levels[w * 32 + j] = L + 1;
           }
           if (lane == j) found = true;
           break;
@@ -251,51 +315,12 @@ __device__ void pull_round(const BfsParams &p, int L, Acc &acc) {
       }
     }
     const unsigned m = __ballot_sync(kFull, found);
-    if (lane == 0 && m) p.nxt[w] = m;
+    if (lane == 0 && m) nxt[w] = m;
     if (found) {
       acc.nf += 1;
       acc.visdeg += (unsigned long long)(e - s);
     }
   }
-}
-
-// visited |= next; frontier = next; next = 0.  When the next round pushes
-// after a pull round, the new frontier's queue is built here as well.
-__device__ void update_round(const BfsParams &p, int L, bool build_queue, RoundRec *Rn,
-                             Acc &acc) {
-  const int lane = lane_id();
-  const int gw = warp_id_global();
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int next_parity = (L + 1) & 1;
-  for (int64_t w0 = (int64_t)gw * 32; w0 < p.words; w0 += (int64_t)nwarps * 32) {
-    const int64_t w = w0 + lane;
-    uint32_t bits = 0;
-    if (w < p.words) {
-      bits = p.nxt[w];
-      if (bits) {
-        p.vis[w] |= bits;
-        p.nxt[w] = 0;
-      }
-      p.cur[w] = bits;
-    }
-    if (build_queue) {
-      uint32_t rest = bits;
-      while (__ballot_sync(kFull, rest != 0)) {
-        bool claimed = rest != 0;
-        int32_t v = 0;
-        int64_t deg = 0;
-        if (claimed) {
-          const int b = __ffs(rest) - 1;
-          rest &= rest - 1u;
-          v = (int32_t)(w * 32 + b);
-          deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
-        }
-        Acc scratch;  // counts of this frontier were taken in the pull round
-        enqueue_claims(p, claimed, v, deg, next_parity, Rn, scratch);
-      }
-    }
-  }
-  (void)acc;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
@@ -363,6 +388,7 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
   const int32_t root = (int32_t)p.root;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
   const long long t_start = leader ? global_ns() : 0;
+  uint32_t *fr[3] = {p.fr0, p.fr1, p.fr2};
 
   // ---- phase 0: start_spmv -- reset outputs and bitmaps, seed the root ----
   for (int64_t i = gtid; i < p.n; i += nthreads) {
@@ -370,10 +396,10 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
     p.parents[i] = (i == root) ? root : -1;
   }
   for (int64_t w = gtid; w < p.words; w += nthreads) {
-    const uint32_t bit = (w == (root >> 5)) ? (1u << (root & 31)) : 0u;
-    p.vis[w] = bit;
-    p.cur[w] = bit;
-    p.nxt[w] = 0;
+    p.vis[w] = 0;
+    p.fr0[w] = (w == (root >> 5)) ? (1u << (root & 31)) : 0u;
+    p.fr1[w] = 0;
+    p.fr2[w] = 0;
   }
   if (leader) {
     const int64_t deg = p.out_off[root + 1] - p.out_off[root];
@@ -384,17 +410,16 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
     if (deg <= kLightMax) {
       p.queue0[0] = root;
       R0->nlight = 1;
-    } else if (deg <= kMediumMax) {
-      p.queue0[p.n - 1] = root;
-      R0->nmedium = 1;
     } else {
-      p.heavy0[0] = root;
-      R0->nheavy = 1;
+      p.queue0[p.n - 1] = root;
+      p.bigoff0[0] = 0;
+      R0->big = (1ull << 32) | (unsigned long long)deg;
     }
   }
   bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns, p.unmatched_wait ? 1u : 0u);
 
   int dir = kPush;
+  bool queued = true;  // F_L is in a queue (a pull round leaves it in the bitmap only)
   int L = 0;
   int pull_rounds = 0, switches = 0;
   unsigned long long prev_nf = 1, visited = 1;
@@ -405,15 +430,34 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
   while (ok) {
     RoundRec *Rc = &ctl->rec[L % kRing];
     RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
-    if (leader && L > 0 && L - 1 < CG_HISTORY) {
-      const long long now = global_ns();
-      p.stats->round_ns[L - 1] = now - t_round;
-      t_round = now;
+    const uint32_t *cur = fr[L % 3];
+    uint32_t *nxt = fr[(L + 1) % 3];
+    uint32_t *old = fr[(L + 2) % 3];
+    if (leader) {
+      if (L > 0 && L - 1 < CG_HISTORY) {
+        const long long now = global_ns();
+        p.stats->round_ns[L - 1] = now - t_round;
+        t_round = now;
+      }
+      RoundRec *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
+      Rz->nf = Rz->mf = Rz->visdeg = Rz->big = 0;
+      Rz->nlight = Rz->work = 0;
     }
-    if (dir == kPush)
-      push_round(p, L, Rc, Rn, acc);
-    else
-      pull_round(p, L, acc);
+    if (dir == kPush) {
+      if (queued)
+        push_round_queue(p, cur, nxt, L, Rc, Rn, acc);
+      else
+        push_round_bitmap(p, cur, nxt, L, Rn, acc);
+    } else {
+      pull_round(p, cur, nxt, L, acc);
+    }
+    // vis |= F_L (readers test vis | F_L, so this races with nothing) and
+    // clear F_{L-1}, which becomes the next round's output bitmap
+    for (int64_t w = gtid; w < p.words; w += nthreads) {
+      const uint32_t c = cur[w];
+      if (c) p.vis[w] |= c;
+      old[w] = 0;
+    }
     flush_acc(acc, Rn);
     if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
 
@@ -438,13 +482,7 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
     }
     const int next = next_direction(p, dir, nf, prev_nf, mf, explored);
     explored += vd;
-    update_round(p, L, next == kPush && dir == kPull, Rn, acc);
-    if (leader) {
-      RoundRec *Rz = &ctl->rec[(L + 2) % kRing];
-      Rz->nf = Rz->mf = Rz->visdeg = 0;
-      Rz->nlight = Rz->nmedium = Rz->nheavy = Rz->work = 0;
-    }
-    if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
+    queued = dir == kPush;  // a push round queued F_{L+1}; a pull round did not
     if (next != dir) ++switches;
     prev_nf = nf;
     dir = next;
@@ -494,23 +532,27 @@ __global__ void count_edges_kernel(int64_t n, int symmetric, const int64_t *__re
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(m_out + blockIdx.y, local);
 }
 
+int64_t bfs_big_capacity(int64_t n, int64_t nnz) {
+  const int64_t c = nnz / (kLightMax + 1) + 1;
+  return c < n ? c : n;
+}
+
 int bfs_prepare(cg_graph *g) {
   if (g->bitmaps) return CG_OK;
   int dev_coop = 0;
   CG_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, g->device));
   if (!dev_coop) return CG_ERR_NOT_SUPPORTED;
   g->words = (g->n + 31) / 32;
-  g->hcap = g->nnz / (kMediumMax + 1) + 1;
-  if (g->hcap > g->n) g->hcap = g->n;
-  size_t bytes_bm = sizeof(uint32_t) * 3 * (size_t)g->words;
-  size_t bytes_q = sizeof(int32_t) * 2 * (size_t)g->n;
-  size_t bytes_h = sizeof(int32_t) * 2 * (size_t)g->hcap;
+  g->bcap = bfs_big_capacity(g->n, g->nnz);
+  const size_t bytes_bm = sizeof(uint32_t) * 4 * (size_t)g->words;
+  const size_t bytes_q = sizeof(int32_t) * 2 * (size_t)g->n;
+  const size_t bytes_b = sizeof(uint32_t) * 2 * (size_t)g->bcap;
   if (cudaMalloc(&g->bitmaps, bytes_bm) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
   if (cudaMalloc(&g->queue, bytes_q) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
-  if (cudaMalloc(&g->heavy, bytes_h) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
+  if (cudaMalloc(&g->bigoff, bytes_b) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
   if (cudaMalloc(&g->ctl, sizeof(BfsCtl)) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
   if (cudaMalloc(&g->d_stats, sizeof(cg_stats)) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
-  g->device_bytes += bytes_bm + bytes_q + bytes_h + sizeof(BfsCtl) + sizeof(cg_stats);
+  g->device_bytes += bytes_bm + bytes_q + bytes_b + sizeof(BfsCtl) + sizeof(cg_stats);
   CG_CUDA(cudaMemsetAsync(g->ctl, 0, sizeof(BfsCtl), g->stream));
   CG_CUDA(cudaMemsetAsync(g->d_stats, 0, sizeof(cg_stats), g->stream));
   return CG_OK;
@@ -543,12 +585,13 @@ int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents)
   p.out_off = g->out_off;
   p.out_idx = g->out_idx;
   p.vis = g->bitmaps;
-  p.cur = g->bitmaps + g->words;
-  p.nxt = g->bitmaps + 2 * g->words;
+  p.fr0 = g->bitmaps + g->words;
+  p.fr1 = g->bitmaps + 2 * g->words;
+  p.fr2 = g->bitmaps + 3 * g->words;
   p.queue0 = g->queue;
   p.queue1 = g->queue + g->n;
-  p.heavy0 = g->heavy;
-  p.heavy1 = g->heavy + g->hcap;
+  p.bigoff0 = g->bigoff;
+  p.bigoff1 = g->bigoff + g->bcap;
   p.levels = d_levels;
   p.parents = d_parents;
   p.ctl = g->ctl;

@@ -5,13 +5,17 @@
 //   out_off int64[n+1], out_idx int32[nnz]   CSC of A (column c = targets of c);
 //                                             aliases of in_* when A is symmetric
 // Per-root search state (allocated once per handle, reused by every search):
-//   vis, cur, nxt  uint32[words]  packed bitmaps (visited, frontier, next frontier);
-//                                 the reference's visited_bitmap / x_bitmap / y_bitmap
+//   vis, fr[3]     uint32[words]  packed bitmaps: visited-before-the-frontier and three
+//                                 rotating frontier bitmaps (round L reads fr[L%3] = F_L,
+//                                 writes fr[(L+1)%3] and clears fr[(L+2)%3]); a vertex
+//                                 counts as visited when its bit is in vis | F_L.  These
+//                                 are the reference's visited_bitmap / x_bitmap / y_bitmap
 //                                 (bool_pe.csl) over all n vertices instead of per PE
-//   queue[2]       int32[n]       push-round frontier queues; light vertices fill
-//                                 from the front, medium ones from the back
-//   heavy[2]       int32[hcap]    vertices whose adjacency is split over the grid
-//   ctl            BfsCtl         per-round counters, grid-wait state, status
+//   queue[2]       int32[n]       push-round frontier queues: light vertices (out-degree
+//                                 <= kLightMax) from the front, big ones from the back
+//   bigoff[2]      uint32[bcap]   prefix offsets of the big vertices' edge lists, in
+//                                 queue order (edge-balanced chunking)
+//   ctl            BfsCtl         per-round records, grid-wait counter, status
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -22,7 +26,8 @@ namespace cg {
 
 // Degree classes of a push-round frontier vertex.
 constexpr int kLightMax = 64;     // <= this: 32 vertices share one warp (edge-balanced)
-constexpr int kMediumMax = 4096;  // <= this: one warp per vertex; above: whole grid
+constexpr int kMediumMax = 4096;  // multi-source push: <= this one warp, above: whole grid
+constexpr int kPushChunk = 1024;  // edges of big frontier vertices per work item
 
 constexpr int kRing = 4;          // per-round record ring (rounds L .. L+3)
 
@@ -31,11 +36,10 @@ struct RoundRec {
   unsigned long long nf;       // |F_k|
   unsigned long long mf;       // sum of out-degrees over F_k
   unsigned long long visdeg;   // sum of degrees over F_k (for unexplored-edge count)
-  unsigned int nlight;         // queue front
-  unsigned int nmedium;        // queue back
-  unsigned int nheavy;         // heavy list
+  unsigned long long big;      // (count << 32) | total edges of the big vertices of F_k
+  unsigned int nlight;         // light vertices, queue front
   unsigned int work;           // dynamic work counter used while F_k is expanded
-  unsigned long long pad[4];
+  unsigned long long pad[3];
 };
 
 struct GridWait {
@@ -61,9 +65,9 @@ struct BfsParams {
   const int32_t *__restrict__ in_idx;
   const int64_t *__restrict__ out_off;
   const int32_t *__restrict__ out_idx;
-  uint32_t *vis, *cur, *nxt;
+  uint32_t *vis, *fr0, *fr1, *fr2;
   int32_t *queue0, *queue1;
-  int32_t *heavy0, *heavy1;
+  uint32_t *bigoff0, *bigoff1;
   int32_t *levels, *parents;
   BfsCtl *ctl;
   cg_stats *stats;
@@ -91,10 +95,10 @@ struct cg_graph {
   cg_options opt{};
   // per-root search state
   int64_t words = 0;
-  uint32_t *bitmaps = nullptr;  // vis | cur | nxt, 3 * words
+  uint32_t *bitmaps = nullptr;  // vis | fr0 | fr1 | fr2, 4 * words
   int32_t *queue = nullptr;     // 2 * n
-  int32_t *heavy = nullptr;     // 2 * hcap
-  int64_t hcap = 0;
+  uint32_t *bigoff = nullptr;   // 2 * bcap
+  int64_t bcap = 0;
   cg::BfsCtl *ctl = nullptr;
   cg_stats *d_stats = nullptr;
   int32_t *tmp_levels = nullptr;   // host-output searches land here first
@@ -137,42 +141,49 @@ __device__ __forceinline__ long long global_ns() {
   return t;
 }
 
-// Grid-wide wait for a cooperative launch (all blocks co-resident).  Every
-// wait is bounded: after `timeout_ns` (or once another block has flagged an
-// error) the block records CG_ERR_TIMEOUT and the caller leaves its loop, so
-// a wait that can never complete ends the kernel instead of spinning.
-// `extra` > 0 makes the wait expect that many arrivals that never come (the
-// test hook behind cg_options.test_unmatched_wait).
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide wait for a cooperative launch (all blocks co-resident).  Thread 0
+// of each block arrives with an acquire-release add on the counter (releasing
+// the block's writes, ordered before it by __syncthreads); the last arrival
+// resets the counter and releases the generation word, which the others poll
+// with acquire loads.  Every wait is bounded: after `timeout_ns` (or once
+// another block has flagged an error) the block records CG_ERR_TIMEOUT and the
+// caller leaves its loop, so a wait that can never complete ends the kernel
+// instead of spinning.  `extra` > 0 makes the wait expect that many arrivals
+// that never come (the test hook behind cg_options.test_unmatched_wait).
 __device__ __forceinline__ bool grid_wait(GridWait *w, int *status, long long timeout_ns,
                                           unsigned extra = 0) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned *vgen = &w->gen;
-    unsigned g = *vgen;
-    __threadfence();
-    unsigned target = gridDim.x + extra;
-    unsigned arrived = atomicAdd(&w->count, 1u) + 1u;
-    if (arrived == target) {
-      w->count = 0;
-      __threadfence();
-      atomicAdd(&w->gen, 1u);
+    const unsigned g = ld_acquire(&w->gen);
+    const unsigned target = gridDim.x + extra;
+    unsigned arrived;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
+                 : "=r"(arrived) : "l"(&w->count) : "memory");
+    if (arrived + 1u == target) {
+      asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->count) : "memory");
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&w->gen) : "memory");
     } else {
-      long long t0 = global_ns();
+      long long t0 = 0;
       unsigned spins = 0;
-      while (*vgen == g) {
-        if ((++spins & 63u) == 0) {
+      while (ld_acquire(&w->gen) == g) {
+        if ((++spins & 255u) == 0) {
+          if (t0 == 0) t0 = global_ns();
           if (*(volatile int *)status != 0 || global_ns() - t0 > timeout_ns) {
             atomicCAS(status, 0, (int)CG_ERR_TIMEOUT);
             ok = 0;
             break;
           }
         }
-        __nanosleep(32);
       }
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();

@@ -25,19 +25,21 @@ namespace cg {
 __global__ void bfs_persistent(BfsParams p);
 void set_error_text(const char *text);
 
+int64_t bfs_big_capacity(int64_t n, int64_t nnz);
+
 constexpr int64_t kNoAllocMaxVertices = CG_NOALLOC_MAX_VERTICES;
-constexpr int64_t kNoAllocMaxHeavy = CG_NOALLOC_MAX_HEAVY;
+constexpr int64_t kNoAllocMaxBig = CG_NOALLOC_MAX_BIG;
 constexpr int64_t kNoAllocWords = (kNoAllocMaxVertices + 31) / 32;
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffCtl = 0;
 constexpr size_t kOffStats = align256(kOffCtl + sizeof(BfsCtl));
 constexpr size_t kOffBitmaps = align256(kOffStats + sizeof(cg_stats));
-constexpr size_t kOffQueue = align256(kOffBitmaps + sizeof(uint32_t) * 3 * kNoAllocWords);
-constexpr size_t kOffHeavy = align256(kOffQueue + sizeof(int32_t) * 2 * kNoAllocMaxVertices);
-constexpr size_t kScratchBytes = align256(kOffHeavy + sizeof(int32_t) * 2 * kNoAllocMaxHeavy);
+constexpr size_t kOffQueue = align256(kOffBitmaps + sizeof(uint32_t) * 4 * kNoAllocWords);
+constexpr size_t kOffBig = align256(kOffQueue + sizeof(int32_t) * 2 * kNoAllocMaxVertices);
+constexpr size_t kScratchBytes = align256(kOffBig + sizeof(uint32_t) * 2 * kNoAllocMaxBig);
 
-// The search state of every cg_bfs_noalloc call on this GPU (about 17 MiB).
+// The search state of every cg_bfs_noalloc call on this GPU (about 25 MiB).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
@@ -78,14 +80,13 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   if (n <= 0 || nnz < 0 || !d_in_off || (nnz > 0 && !d_in_idx) || !d_levels || !d_parents ||
       root < 0 || root >= n || ((d_out_off == nullptr) != (d_out_idx == nullptr)))
     return CG_ERR_INVALID_ARG;
-  const int64_t hcap = nnz / (kMediumMax + 1) + 1;
-  if (n > kNoAllocMaxVertices || (hcap < n ? hcap : n) > kNoAllocMaxHeavy) {
+  if (n > kNoAllocMaxVertices || bfs_big_capacity(n, nnz) > kNoAllocMaxBig) {
     char msg[200];
     snprintf(msg, sizeof(msg),
              "cg_bfs_noalloc: graph exceeds the fixed scratch capacity (n = %lld > %lld "
-             "vertices, or more than %lld vertices of out-degree > %d)",
-             (long long)n, (long long)kNoAllocMaxVertices, (long long)kNoAllocMaxHeavy,
-             kMediumMax);
+             "vertices, or nnz / %d + 1 > %lld vertices of out-degree > %d)",
+             (long long)n, (long long)kNoAllocMaxVertices, kLightMax + 1,
+             (long long)kNoAllocMaxBig, kLightMax);
     set_error_text(msg);
     return CG_ERR_INVALID_ARG;
   }
@@ -110,14 +111,15 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   p.out_idx = d_out_idx ? d_out_idx : d_in_idx;
   uint32_t *bitmaps = reinterpret_cast<uint32_t *>(base + kOffBitmaps);
   p.vis = bitmaps;
-  p.cur = bitmaps + words;
-  p.nxt = bitmaps + 2 * words;
+  p.fr0 = bitmaps + words;
+  p.fr1 = bitmaps + 2 * words;
+  p.fr2 = bitmaps + 3 * words;
   int32_t *queue = reinterpret_cast<int32_t *>(base + kOffQueue);
   p.queue0 = queue;
   p.queue1 = queue + n;
-  int32_t *heavy = reinterpret_cast<int32_t *>(base + kOffHeavy);
-  p.heavy0 = heavy;
-  p.heavy1 = heavy + kNoAllocMaxHeavy;
+  uint32_t *bigoff = reinterpret_cast<uint32_t *>(base + kOffBig);
+  p.bigoff0 = bigoff;
+  p.bigoff1 = bigoff + kNoAllocMaxBig;
   p.levels = d_levels;
   p.parents = d_parents;
   p.ctl = reinterpret_cast<BfsCtl *>(base + kOffCtl);

@@ -209,11 +209,11 @@ int cg_graph_export(const cg_graph *g, int64_t *in_off, int32_t *in_idx, int64_t
  * synchronisation a cudaMalloc or cudaFree implies.  The caller passes its own
  * device CSR (and CSC, or NULL for a symmetric A) and device outputs of n
  * int32 each; the search state lives in one fixed __device__ array of this
- * library (about 17 MiB, present on every GPU that loads the library until
+ * library (about 25 MiB, present on every GPU that loads the library until
  * the process exits).  Nothing is allocated: no cudaMalloc, cudaFree or
  * allocating library routine is called.
- * Limits: n <= CG_NOALLOC_MAX_VERTICES and nnz / 4097 + 1 (the bound on
- * vertices of out-degree > 4096) <= CG_NOALLOC_MAX_HEAVY; larger graphs are
+ * Limits: n <= CG_NOALLOC_MAX_VERTICES and min(n, nnz / 65 + 1) (the bound on
+ * vertices of out-degree > 64) <= CG_NOALLOC_MAX_BIG; larger graphs are
  * rejected with CG_ERR_INVALID_ARG and a message in cg_last_error_string.
  * Every call on a GPU shares the array and it keeps the last call's contents:
  * calls that overlap on that GPU (other streams or threads) race and give
@@ -222,7 +222,7 @@ int cg_graph_export(const cg_graph *g, int64_t *in_off, int32_t *in_idx, int64_t
  * alpha = 15, beta = 18.  With stats != NULL the call waits for `stream` and
  * returns the search's status; with NULL it returns once the work is queued. */
 #define CG_NOALLOC_MAX_VERTICES (1 << 21)
-#define CG_NOALLOC_MAX_HEAVY (1 << 15)
+#define CG_NOALLOC_MAX_BIG (1 << 20)
 int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off, const int32_t *d_in_idx,
                    const int64_t *d_out_off, const int32_t *d_out_idx, int64_t root,
                    int32_t *d_levels, int32_t *d_parents, cg_stats *stats, void *stream);
