@@ -187,13 +187,16 @@ __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32
   const unsigned nbig = (unsigned)(bigw >> 32);
   const unsigned big_edges = (unsigned)(bigw & 0xffffffffu);
   const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
-  const unsigned nchunks = (big_edges + kPushChunk - 1) / kPushChunk;
+  // chunks of 32 .. kPushChunk edges: small frontiers still spread over the grid
+  unsigned chunk = ((big_edges / (unsigned)nwarps) + 31u) & ~31u;
+  chunk = chunk < 32u ? 32u : (chunk > (unsigned)kPushChunk ? (unsigned)kPushChunk : chunk);
+  const unsigned nchunks = (big_edges + chunk - 1) / chunk;
   const unsigned nitems = nchunks + (nlight + 31u) / 32u;
   unsigned item = (unsigned)warp_id_global();
   while (item < nitems) {
     if (item < nchunks) {
-      const unsigned x0 = item * kPushChunk;
-      const unsigned x1 = min(x0 + (unsigned)kPushChunk, big_edges);
+      const unsigned x0 = item * chunk;
+      const unsigned x1 = min(x0 + chunk, big_edges);
       // big vertex j holding edge position x0: the last j with boff[j] <= x0
       unsigned lo = 0, hi = nbig - 1;
       while (lo < hi) {
@@ -350,12 +353,36 @@ __device__ void flush_acc(Acc &acc, RoundRec *Rn) {
     b = warp_sum(b);
     c = warp_sum(c);
     if (lane == 0) {
-      if (a) atomicAdd(&Rn->nf, a);
-      if (b) atomicAdd(&Rn->mf, b);
-      if (c) atomicAdd(&Rn->visdeg, c);
+      const int sh = blockIdx.x % kCounterShards;
+      if (a) atomicAdd(&Rn->nf[sh], a);
+      if (b) atomicAdd(&Rn->mf[sh], b);
+      if (c) atomicAdd(&Rn->visdeg[sh], c);
     }
   }
   acc = Acc();
+}
+
+// Totals of the sharded round counters, read after a grid-wide wait (all
+// threads of the block call; the result is the same in every block).
+__device__ void read_counters(const RoundRec *R, unsigned long long &nf, unsigned long long &mf,
+                              unsigned long long &vd) {
+  __shared__ unsigned long long s_tot[3];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int which = lane / kCounterShards, sh = lane % kCounterShards;
+    unsigned long long x = 0;
+    if (which == 0) x = *(volatile const unsigned long long *)&R->nf[sh];
+    else if (which == 1) x = *(volatile const unsigned long long *)&R->mf[sh];
+    else if (which == 2) x = *(volatile const unsigned long long *)&R->visdeg[sh];
+#pragma unroll
+    for (int o = kCounterShards / 2; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+    if (sh == 0 && which < 3) s_tot[which] = x;
+  }
+  __syncthreads();
+  nf = s_tot[0];
+  mf = s_tot[1];
+  vd = s_tot[2];
+  __syncthreads();
 }
 
 __device__ __forceinline__ int next_direction(const BfsParams &p, int dir, unsigned long long nf,
@@ -404,9 +431,9 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
   if (leader) {
     const int64_t deg = p.out_off[root + 1] - p.out_off[root];
     RoundRec *R0 = &ctl->rec[0];
-    R0->nf = 1;
-    R0->mf = deg;
-    R0->visdeg = deg;
+    R0->nf[0] = 1;
+    R0->mf[0] = deg;
+    R0->visdeg[0] = deg;
     if (deg <= kLightMax) {
       p.queue0[0] = root;
       R0->nlight = 1;
@@ -440,7 +467,8 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
         t_round = now;
       }
       RoundRec *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
-      Rz->nf = Rz->mf = Rz->visdeg = Rz->big = 0;
+      for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->mf[i] = Rz->visdeg[i] = 0;
+      Rz->big = 0;
       Rz->nlight = Rz->work = 0;
     }
     if (dir == kPush) {
@@ -461,9 +489,8 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
     flush_acc(acc, Rn);
     if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
 
-    const unsigned long long nf = *(volatile unsigned long long *)&Rn->nf;
-    const unsigned long long mf = *(volatile unsigned long long *)&Rn->mf;
-    const unsigned long long vd = *(volatile unsigned long long *)&Rn->visdeg;
+    unsigned long long nf, mf, vd;
+    read_counters(Rn, nf, mf, vd);
     if (leader && L < CG_HISTORY) {
       p.stats->nf_history[L] = (int64_t)nf;
       p.stats->direction_history[L] = dir;

@@ -24,6 +24,26 @@
 
 namespace cg {
 
+// Grid-wide wait state: blocks arrive on one of kWaitGroups group counters
+// (blockIdx % kWaitGroups), the last of each group on the top counter, the
+// last group releases the generation word.  Each counter has its own
+// 128-byte line so arrivals of different groups do not serialise.
+constexpr int kWaitGroups = 16;
+struct GridWaitGroup {
+  unsigned int count;
+  unsigned int pad[31];
+};
+struct GridWait {
+  unsigned int top;
+  unsigned int gen;
+  unsigned int pad[30];
+  GridWaitGroup group[kWaitGroups];
+};
+
+// Round counters are sharded over kCounterShards addresses (blockIdx % shards)
+// so that block flushes do not all land on one address.
+constexpr int kCounterShards = 8;
+
 // Degree classes of a push-round frontier vertex.
 constexpr int kLightMax = 64;     // <= this: 32 vertices share one warp (edge-balanced)
 constexpr int kMediumMax = 4096;  // multi-source push: <= this one warp, above: whole grid
@@ -33,19 +53,13 @@ constexpr int kRing = 4;          // per-round record ring (rounds L .. L+3)
 
 // Statistics of frontier F_k (the vertices at level k) and the queue holding it.
 struct RoundRec {
-  unsigned long long nf;       // |F_k|
-  unsigned long long mf;       // sum of out-degrees over F_k
-  unsigned long long visdeg;   // sum of degrees over F_k (for unexplored-edge count)
+  unsigned long long nf[kCounterShards];      // |F_k|
+  unsigned long long mf[kCounterShards];      // sum of out-degrees over F_k
+  unsigned long long visdeg[kCounterShards];  // sum of degrees over F_k (unexplored edges)
   unsigned long long big;      // (count << 32) | total edges of the big vertices of F_k
   unsigned int nlight;         // light vertices, queue front
   unsigned int work;           // dynamic work counter used while F_k is expanded
-  unsigned long long pad[3];
-};
-
-struct GridWait {
-  unsigned int count;
-  unsigned int gen;
-  unsigned int pad[30];
+  unsigned long long pad[6];
 };
 
 struct BfsCtl {
@@ -148,14 +162,23 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 }
 
 // Grid-wide wait for a cooperative launch (all blocks co-resident).  Thread 0
-// of each block arrives with an acquire-release add on the counter (releasing
-// the block's writes, ordered before it by __syncthreads); the last arrival
-// resets the counter and releases the generation word, which the others poll
-// with acquire loads.  Every wait is bounded: after `timeout_ns` (or once
-// another block has flagged an error) the block records CG_ERR_TIMEOUT and the
-// caller leaves its loop, so a wait that can never complete ends the kernel
-// instead of spinning.  `extra` > 0 makes the wait expect that many arrivals
-// that never come (the test hook behind cg_options.test_unmatched_wait).
+// of each block arrives on its group counter with an acquire-release add
+// (releasing the block's writes, ordered before it by __syncthreads); the last
+// arrival of a group resets that counter and arrives on the top counter the
+// same way; the last group resets the top counter and releases the
+// generation word, which everyone else polls with acquire loads.  Every wait
+// is bounded: after `timeout_ns` (or once another block has flagged an error)
+// the block records CG_ERR_TIMEOUT and the caller leaves its loop, so a wait
+// that can never complete ends the kernel instead of spinning.  `extra` > 0
+// makes the top counter expect that many arrivals that never come (the test
+// hook behind cg_options.test_unmatched_wait).
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
+               : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 __device__ __forceinline__ bool grid_wait(GridWait *w, int *status, long long timeout_ns,
                                           unsigned extra = 0) {
   __shared__ int s_ok;
@@ -163,14 +186,19 @@ __device__ __forceinline__ bool grid_wait(GridWait *w, int *status, long long ti
   if (threadIdx.x == 0) {
     int ok = 1;
     const unsigned g = ld_acquire(&w->gen);
-    const unsigned target = gridDim.x + extra;
-    unsigned arrived;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;"
-                 : "=r"(arrived) : "l"(&w->count) : "memory");
-    if (arrived + 1u == target) {
-      asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->count) : "memory");
-      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&w->gen) : "memory");
-    } else {
+    const unsigned groups = gridDim.x < (unsigned)kWaitGroups ? gridDim.x : kWaitGroups;
+    const unsigned grp = blockIdx.x % kWaitGroups;
+    const unsigned members = (gridDim.x - grp + kWaitGroups - 1) / kWaitGroups;
+    bool released = false;
+    if (atom_add_acq_rel(&w->group[grp].count, 1u) + 1u == members) {
+      asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->group[grp].count) : "memory");
+      if (atom_add_acq_rel(&w->top, 1u) + 1u == groups + extra) {
+        asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->top) : "memory");
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&w->gen) : "memory");
+        released = true;
+      }
+    }
+    if (!released) {
       long long t0 = 0;
       unsigned spins = 0;
       while (ld_acquire(&w->gen) == g) {

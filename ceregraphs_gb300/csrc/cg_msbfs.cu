@@ -14,15 +14,21 @@
 //   fr[3]        frontier masks: round L reads fr[L % 3] (F_L), writes
 //                fr[(L+1) % 3] (F_{L+1}) and clears fr[(L+2) % 3] (F_{L-1})
 //   touched[2]   1 bit per vertex: "already queued this round" (push rounds)
-//   queue[2]     vertex queues of the frontier (any lane set), light from the
-//                front, medium from the back; heavy[2] for grid-split lists
+//   queue[2]     frontier vertices (any lane set): light from the front, big
+//                (out-degree > kLightMax) from the back with edge prefix offsets
+// Hubs (in-degree > kHubDeg; a fixed list per graph) never have their in-list
+// walked by one warp: each round their in-list is cut into kHubChunk pieces
+// scanned by different warps, which combine per-lane parent candidates with
+// atomicMin in a small per-hub buffer; a finalize phase then writes the hub's
+// outputs and queues it (hubq[2], a separate frontier list).
 //
-// Pull round: every vertex with unvisited lanes scans its ascending in-list
-// and takes, per lane, the first frontier source (the minimum); it stops once
-// every wanted lane is found.  Push round: frontier vertices OR their masks
-// into their out-neighbours' next masks (atomicOr), then a resolve phase
-// scans each newly reached vertex's ascending in-list for its parents -- no
-// atomics on the per-lane parent arrays in either direction.
+// Pull round: every non-hub vertex with unvisited lanes whose search is still
+// running scans its ascending in-list and takes, per lane, the first frontier
+// source (the minimum), stopping once every wanted lane is found; hubs go
+// through the chunks.  Push round: frontier vertices OR their masks into
+// their out-neighbours' next masks (atomicOr); hub targets get parent
+// candidates by atomicMin instead; a resolve phase scans each newly reached
+// non-hub vertex's ascending in-list for its parents.
 #include <cuda_runtime.h>
 
 #include "cg_internal.cuh"
@@ -32,18 +38,20 @@ namespace cg {
 constexpr unsigned kMsFull = 0xffffffffu;
 constexpr int kMsBlock = 512;
 constexpr int kMsMaxLanes = 128;
+constexpr int kPullLight = 32;    // in-degree <= this: one thread scans the in-list
+constexpr int kHubDeg = 1024;     // in-degree > this: hub
+constexpr int kHubChunk = 1024;   // in-list entries of a hub per work item
 
 struct MsRound {
-  unsigned long long nf;      // vertices with a nonzero frontier mask
-  unsigned long long visits;  // lane discoveries
-  unsigned long long mf;      // sum of out-degrees over the frontier vertices
-  unsigned int nlight, nmedium, nheavy, work;
+  unsigned long long nf[kCounterShards];      // vertices with a nonzero frontier mask
+  unsigned long long visits[kCounterShards];  // lane discoveries
+  unsigned long long mf[kCounterShards];      // sum of out-degrees over the frontier
+  unsigned long long big;       // main queue: (count << 32) | edges of its big vertices
+  unsigned long long hub;       // hub queue:  (count << 32) | edges
+  unsigned int nlight, work;
   unsigned long long lanes[2];  // lanes whose frontier is non-empty
-  unsigned long long pad;
+  unsigned long long pad[2];
 };
-
-// In-degree above which a vertex's in-list is scanned by a whole warp.
-constexpr int kPullLight = 32;
 
 struct MsCtl {
   GridWait wait;
@@ -60,7 +68,16 @@ struct MsParams {
   const int32_t *__restrict__ out_idx;
   uint64_t *vis, *fr0, *fr1, *fr2;
   uint32_t *touched0, *touched1;
-  int32_t *queue0, *queue1, *heavy0, *heavy1;
+  int32_t *queue0, *queue1;
+  uint32_t *bigoff0, *bigoff1;
+  int32_t *hubq0, *hubq1;
+  uint32_t *huboff0, *huboff1;
+  const int32_t *hub_slot;   // [n], -1 for non-hubs
+  const int32_t *hub_vtx;    // [nhub]
+  const uint32_t *hub_choff; // [nhub + 1] prefix of in-list chunks
+  uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
+  uint64_t *hub_found;       // [nhub][W] lanes found this round
+  int nhub;
   int32_t *levels, *parents;  // root-major, k x n
   MsCtl *ctl;
   cg_stats *stats;
@@ -154,6 +171,15 @@ __device__ __forceinline__ Mask<W> lane_mask(int k) {
   return m;
 }
 
+template <int W>
+__device__ __forceinline__ Mask<W> warp_or(Mask<W> m) {
+#pragma unroll
+  for (int j = 0; j < W; ++j)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m.w[j] |= __shfl_xor_sync(kMsFull, m.w[j], o);
+  return m;
+}
+
 // Writes level and parent of vertex v for every lane in `m`.
 template <int W>
 __device__ __forceinline__ void write_lanes(const MsParams &p, int64_t v, const Mask<W> &m,
@@ -176,34 +202,49 @@ struct MsAcc {
   unsigned long long lanes[2] = {0ull, 0ull};
 };
 
-// Appends claimed vertices to the next frontier's queue (all lanes call).
-__device__ __forceinline__ void ms_enqueue(const MsParams &p, bool claimed, int32_t v,
-                                           int64_t deg, int next_parity, MsRound *Rn,
-                                           MsAcc &acc) {
+template <int W>
+__device__ __forceinline__ void acc_lanes(MsAcc &acc, const Mask<W> &m) {
+#pragma unroll
+  for (int i = 0; i < W; ++i) acc.lanes[i] |= m.w[i];
+}
+
+// Appends claimed vertices to a frontier list: light ones at the front of
+// `q`, big ones (out-degree > kLightMax) at the back with the prefix offset of
+// their edge lists (one packed atomic per warp: count << 32 | edges).  All 32
+// lanes call.
+__device__ __forceinline__ void ms_enqueue(bool claimed, int32_t v, int64_t deg, int32_t *q,
+                                           int64_t qcap, uint32_t *boff, unsigned *nlight,
+                                           unsigned long long *big, MsAcc &acc) {
   const int lane = lane_id();
   if (!__ballot_sync(kMsFull, claimed)) return;
-  const int cls = !claimed ? -1 : (deg <= kLightMax ? 0 : (deg <= kMediumMax ? 1 : 2));
-  int32_t *q = next_parity ? p.queue1 : p.queue0;
-  int32_t *h = next_parity ? p.heavy1 : p.heavy0;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const unsigned m = __ballot_sync(kMsFull, cls == c);
-    if (!m) continue;
-    const int leader = __ffs(m) - 1;
+  const bool light = claimed && deg <= kLightMax;
+  const bool heavy = claimed && deg > kLightMax;
+  const unsigned below = (1u << lane) - 1u;
+  const unsigned ml = __ballot_sync(kMsFull, light);
+  if (ml) {
+    const int leader = __ffs(ml) - 1;
     unsigned base = 0;
-    if (lane == leader) {
-      unsigned *ctr = c == 0 ? &Rn->nlight : (c == 1 ? &Rn->nmedium : &Rn->nheavy);
-      base = atomicAdd(ctr, (unsigned)__popc(m));
-    }
+    if (lane == leader) base = atomicAdd(nlight, (unsigned)__popc(ml));
     base = __shfl_sync(kMsFull, base, leader);
-    if (cls == c) {
-      const unsigned pos = base + __popc(m & ((1u << lane) - 1u));
-      if (c == 0)
-        q[pos] = v;
-      else if (c == 1)
-        q[p.n - 1 - (int64_t)pos] = v;
-      else
-        h[pos] = v;
+    if (light) q[base + __popc(ml & below)] = v;
+  }
+  const unsigned mb = __ballot_sync(kMsFull, heavy);
+  if (mb) {
+    const unsigned d = heavy ? (unsigned)deg : 0u;
+    unsigned incl = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(kMsFull, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const unsigned total = __shfl_sync(kMsFull, incl, 31);
+    unsigned long long old = 0;
+    if (lane == 0) old = atomicAdd(big, ((unsigned long long)__popc(mb) << 32) | total);
+    old = __shfl_sync(kMsFull, old, 0);
+    if (heavy) {
+      const unsigned idx = (unsigned)(old >> 32) + __popc(mb & below);
+      q[qcap - 1 - (int64_t)idx] = v;
+      boff[idx] = (unsigned)(old & 0xffffffffu) + incl - d;
     }
   }
   if (claimed) {
@@ -248,9 +289,10 @@ __device__ void ms_flush(MsAcc &acc, MsRound *Rn) {
     b = ms_warp_sum(lane < nw ? s_red[1][lane] : 0ull);
     c = ms_warp_sum(lane < nw ? s_red[2][lane] : 0ull);
     if (lane == 0) {
-      if (a) atomicAdd(&Rn->nf, a);
-      if (b) atomicAdd(&Rn->visits, b);
-      if (c) atomicAdd(&Rn->mf, c);
+      const int sh = blockIdx.x % kCounterShards;
+      if (a) atomicAdd(&Rn->nf[sh], a);
+      if (b) atomicAdd(&Rn->visits[sh], b);
+      if (c) atomicAdd(&Rn->mf[sh], c);
       if (s_lanes[0]) atomicOr(&Rn->lanes[0], s_lanes[0]);
       if (s_lanes[1]) atomicOr(&Rn->lanes[1], s_lanes[1]);
     }
@@ -259,22 +301,39 @@ __device__ void ms_flush(MsAcc &acc, MsRound *Rn) {
   acc = MsAcc();
 }
 
-template <int W>
-__device__ __forceinline__ void acc_lanes(MsAcc &acc, const Mask<W> &m) {
+// Totals of the sharded round counters after a grid-wide wait (all threads of
+// the block call; every block gets the same values).
+__device__ void ms_read_counters(const MsRound *R, unsigned long long &nf,
+                                 unsigned long long &visits, unsigned long long &mf) {
+  __shared__ unsigned long long s_tot[3];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int which = lane / kCounterShards, sh = lane % kCounterShards;
+    unsigned long long x = 0;
+    if (which == 0) x = *(volatile const unsigned long long *)&R->nf[sh];
+    else if (which == 1) x = *(volatile const unsigned long long *)&R->visits[sh];
+    else if (which == 2) x = *(volatile const unsigned long long *)&R->mf[sh];
 #pragma unroll
-  for (int i = 0; i < W; ++i) acc.lanes[i] |= m.w[i];
+    for (int o = kCounterShards / 2; o > 0; o >>= 1) x += __shfl_xor_sync(kMsFull, x, o);
+    if (sh == 0 && which < 3) s_tot[which] = x;
+  }
+  __syncthreads();
+  nf = s_tot[0];
+  visits = s_tot[1];
+  mf = s_tot[2];
+  __syncthreads();
 }
 
-// Warp-cooperative scan of vertex v's ascending in-list (all 32 lanes call
-// with the same v and want): 32 sources per step; for each lane bit found in
-// a step, the lowest warp lane holding it -- the smallest source -- is the
-// parent.  Stops once every wanted bit is found.  Returns the found bits.
+// Warp-cooperative scan of in-list entries [s, e) of vertex v (all lanes call
+// with the same arguments): 32 sources per step; for each lane bit found in a
+// step, the lowest warp lane holding it -- the smallest source -- wins.  Stops
+// once every wanted bit is found.  With hub >= 0 the winners go to the hub's
+// candidate buffer by atomicMin; otherwise they are written as outputs.
 template <int W>
-__device__ Mask<W> warp_scan_in_list(const MsParams &p, int64_t v, const Mask<W> &want,
-                                     const uint64_t *cur, int level) {
+__device__ Mask<W> warp_scan(const MsParams &p, int64_t v, int64_t s, int64_t e,
+                             const Mask<W> &want, const uint64_t *cur, int level, int hub) {
   const int lane = lane_id();
   Mask<W> got = Mask<W>::zero();
-  const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
   for (int64_t base = s; base < e; base += 32) {
     const int64_t i = base + lane;
     Mask<W> f = Mask<W>::zero();
@@ -283,11 +342,7 @@ __device__ Mask<W> warp_scan_in_list(const MsParams &p, int64_t v, const Mask<W>
       u = __ldg(p.in_idx + i);
       f = (ld_mask<W>(cur, u) & want).andnot(got);
     }
-    Mask<W> F = f;
-#pragma unroll
-    for (int j = 0; j < W; ++j)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) F.w[j] |= __shfl_xor_sync(kMsFull, F.w[j], o);
+    const Mask<W> F = warp_or<W>(f);
     if (F.any()) {
 #pragma unroll
       for (int j = 0; j < W; ++j) {
@@ -297,9 +352,13 @@ __device__ Mask<W> warp_scan_in_list(const MsParams &p, int64_t v, const Mask<W>
           bits &= bits - 1;
           const unsigned who = __ballot_sync(kMsFull, (f.w[j] >> b) & 1ull);
           if (lane == __ffs(who) - 1) {
-            const int64_t at = (int64_t)(j * 64 + b) * p.n + v;
-            p.levels[at] = level;
-            p.parents[at] = u;
+            if (hub >= 0) {
+              atomicMin(p.hub_cand + (int64_t)hub * (64 * W) + j * 64 + b, (unsigned)u);
+            } else {
+              const int64_t at = (int64_t)(j * 64 + b) * p.n + v;
+              p.levels[at] = level;
+              p.parents[at] = u;
+            }
           }
         }
       }
@@ -312,11 +371,10 @@ __device__ Mask<W> warp_scan_in_list(const MsParams &p, int64_t v, const Mask<W>
 
 // Thread-level scan of the same kind, for short in-lists.
 template <int W>
-__device__ __forceinline__ Mask<W> thread_scan_in_list(const MsParams &p, int64_t v,
-                                                       const Mask<W> &want,
-                                                       const uint64_t *cur, int level) {
+__device__ __forceinline__ Mask<W> thread_scan(const MsParams &p, int64_t v, int64_t s, int64_t e,
+                                               const Mask<W> &want, const uint64_t *cur,
+                                               int level) {
   Mask<W> got = Mask<W>::zero();
-  const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
   for (int64_t i = s; i < e; ++i) {
     const int32_t u = __ldg(p.in_idx + i);
     const Mask<W> f = (ld_mask<W>(cur, u) & want).andnot(got);
@@ -329,48 +387,133 @@ __device__ __forceinline__ Mask<W> thread_scan_in_list(const MsParams &p, int64_
   return got;
 }
 
-// Scans a warp's 32 vertices: short lists one per thread, long ones by the
-// whole warp in turn.  want must be zero for vertices that need no scan.
+// Scans a warp's 32 non-hub vertices: short in-lists one per thread, the
+// others by the whole warp in turn.  want must be zero where no scan is due.
 template <int W>
-__device__ __forceinline__ Mask<W> scan_group(const MsParams &p, int64_t v, const Mask<W> &want,
-                                              const uint64_t *cur, int level) {
+__device__ __forceinline__ Mask<W> scan_group(const MsParams &p, int64_t v, int64_t s, int64_t e,
+                                              const Mask<W> &want, const uint64_t *cur,
+                                              int level) {
   const bool need = want.any();
-  const int64_t deg = need ? (__ldg(p.in_off + v + 1) - __ldg(p.in_off + v)) : 0;
-  const bool heavy = need && deg > kPullLight;
+  const bool longer = need && (e - s) > kPullLight;
   Mask<W> got = Mask<W>::zero();
-  if (need && !heavy) got = thread_scan_in_list<W>(p, v, want, cur, level);
-  unsigned hm = __ballot_sync(kMsFull, heavy);
+  if (need && !longer) got = thread_scan<W>(p, v, s, e, want, cur, level);
+  unsigned hm = __ballot_sync(kMsFull, longer);
   while (hm) {
     const int j = __ffs(hm) - 1;
     hm &= hm - 1;
     const int64_t vj = __shfl_sync(kMsFull, v, j);
+    const int64_t sj = __shfl_sync(kMsFull, s, j), ej = __shfl_sync(kMsFull, e, j);
     Mask<W> wj;
 #pragma unroll
     for (int i = 0; i < W; ++i) wj.w[i] = __shfl_sync(kMsFull, want.w[i], j);
-    const Mask<W> gj = warp_scan_in_list<W>(p, vj, wj, cur, level);
+    const Mask<W> gj = warp_scan<W>(p, vj, sj, ej, wj, cur, level, -1);
     if (lane_id() == j) got = gj;
   }
   return got;
 }
 
-// Pull round over every vertex with unvisited lanes whose frontier is not
-// empty (`active`: lanes whose search has ended cannot be found any more).
+// Hub in-list chunks of a round: chunk c of hub h scans its slice for the
+// wanted lanes (frozen for the round: nothing writes a hub's vis before its
+// finalize), min-combining winners into the candidate buffer.
+template <int W>
+__device__ void hub_chunks(const MsParams &p, const uint64_t *cur, const Mask<W> &active,
+                           int level) {
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const unsigned nchunks = p.hub_choff[p.nhub];
+  for (unsigned c = (unsigned)warp_id_global(); c < nchunks; c += (unsigned)nwarps) {
+    unsigned lo = 0, hi = (unsigned)p.nhub - 1;
+    while (lo < hi) {
+      const unsigned mid = (lo + hi + 1) >> 1;
+      if (p.hub_choff[mid] <= c)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int h = (int)lo;
+    const int32_t v = p.hub_vtx[h];
+    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v));
+    if (!want.any()) continue;
+    const int64_t s = __ldg(p.in_off + v) + (int64_t)(c - p.hub_choff[h]) * kHubChunk;
+    const int64_t e = min(s + (int64_t)kHubChunk, __ldg(p.in_off + v + 1));
+    const Mask<W> got = warp_scan<W>(p, v, s, e, want, cur, level, h);
+    if (lane_id() == 0) {
+#pragma unroll
+      for (int j = 0; j < W; ++j)
+        if (got.w[j])
+          atomicOr(reinterpret_cast<unsigned long long *>(p.hub_found + (int64_t)h * W + j),
+                   (unsigned long long)got.w[j]);
+    }
+  }
+}
+
+// Hubs reached this round: outputs from the candidates, next mask, vis,
+// queue (hub list of the next frontier); candidates reset for the next round.
+template <int W>
+__device__ void hub_finalize(const MsParams &p, int L, uint64_t *nxt, MsRound *Rn, MsAcc &acc) {
+  const int lane = lane_id();
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int next_parity = (L + 1) & 1;
+  int32_t *hq = next_parity ? p.hubq1 : p.hubq0;
+  uint32_t *hoff = next_parity ? p.huboff1 : p.huboff0;
+  for (int h = warp_id_global(); h < p.nhub; h += nwarps) {
+    const Mask<W> found = ld_mask<W>(p.hub_found, h);
+    if (!found.any()) continue;
+    const int32_t v = p.hub_vtx[h];
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int b = lane + 32 * half;
+        if ((found.w[j] >> b) & 1ull) {
+          uint32_t *cand = p.hub_cand + (int64_t)h * (64 * W) + j * 64 + b;
+          const int64_t at = (int64_t)(j * 64 + b) * p.n + v;
+          p.levels[at] = L + 1;
+          p.parents[at] = (int32_t)*cand;
+          *cand = 0xffffffffu;
+        }
+      }
+    }
+    int64_t deg = 0;
+    if (lane == 0) {
+      st_mask<W>(nxt, v, found);
+      st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | found);
+      st_mask<W>(p.hub_found, h, Mask<W>::zero());
+      acc.visits += (unsigned long long)found.popc();
+      acc_lanes<W>(acc, found);
+      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+    }
+    // every hub is "big" in the hub list (no light section is used)
+    ms_enqueue(lane == 0, v, deg > kLightMax ? deg : kLightMax + 1, hq, p.nhub, hoff,
+               &Rn->work /* unused: hubs are never light */, &Rn->hub, acc);
+  }
+}
+
+// Pull round over every non-hub vertex with unvisited lanes whose search is
+// still running (`active`), and over the hub chunks.
 template <int W>
 __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
                         const Mask<W> &active, MsRound *Rn, MsAcc &acc) {
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
+  int32_t *q = next_parity ? p.queue1 : p.queue0;
+  uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
        base < p.n; base += nthreads) {
     const int64_t v = base + lane_id();
     Mask<W> want = Mask<W>::zero();
     Mask<W> seen = Mask<W>::zero();
+    int64_t s = 0, e = 0;
     if (v < p.n) {
       seen = ld_mask<W>(p.vis, v);
       want = active.andnot(seen);
+      if (want.any()) {
+        s = __ldg(p.in_off + v);
+        e = __ldg(p.in_off + v + 1);
+        if (e - s > kHubDeg) want = Mask<W>::zero();  // a hub: done by chunks
+      }
     }
     if (!__ballot_sync(kMsFull, want.any())) continue;
-    const Mask<W> got = scan_group<W>(p, v, want, cur, L + 1);
+    const Mask<W> got = scan_group<W>(p, v, s, e, want, cur, L + 1);
     bool claimed = false;
     int64_t deg = 0;
     if (got.any()) {
@@ -381,18 +524,38 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       acc_lanes<W>(acc, got);
       deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
     }
-    ms_enqueue(p, claimed, (int32_t)v, deg, next_parity, Rn, acc);
+    ms_enqueue(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
+  if (p.nhub > 0) hub_chunks<W>(p, cur, active, L + 1);
 }
 
-// Edge u -> v of a push round; true for the one thread that queues v.
+// Edge u -> v of a push round.  Hub targets take parent candidates directly;
+// other targets get their lanes ORed into the next mask, and the one thread
+// that first touches v this round queues it.
 template <int W>
-__device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, int32_t v,
-                                         uint64_t *nxt, uint32_t *touched) {
+__device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, int32_t u,
+                                         int32_t v, uint64_t *nxt, uint32_t *touched) {
   const Mask<W> f = fu.andnot(ld_mask<W>(p.vis, v));
   if (!f.any()) return false;
-  const Mask<W> have = ld_mask<W>(nxt, v);
-  const Mask<W> add = f.andnot(have);
+  const int h = p.hub_slot[v];
+  if (h >= 0) {
+    const Mask<W> have = ld_mask<W>(p.hub_found, h);
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      uint64_t bits = f.w[j];
+      while (bits) {
+        const int b = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        atomicMin(p.hub_cand + (int64_t)h * (64 * W) + j * 64 + b, (unsigned)u);
+      }
+      const uint64_t add = f.w[j] & ~have.w[j];
+      if (add)
+        atomicOr(reinterpret_cast<unsigned long long *>(p.hub_found + (int64_t)h * W + j),
+                 (unsigned long long)add);
+    }
+    return false;
+  }
+  const Mask<W> add = f.andnot(ld_mask<W>(nxt, v));
   if (add.any()) {
 #pragma unroll
     for (int i = 0; i < W; ++i)
@@ -407,17 +570,66 @@ __device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, i
 
 template <int W>
 __device__ __forceinline__ void ms_push_step(const MsParams &p, bool valid, const Mask<W> &fu,
-                                             int64_t e, uint64_t *nxt, uint32_t *touched,
-                                             int next_parity, MsRound *Rn, MsAcc &acc) {
+                                             int32_t u, int64_t e, uint64_t *nxt,
+                                             uint32_t *touched, int32_t *q, uint32_t *boff,
+                                             MsRound *Rn, MsAcc &acc) {
   bool claimed = false;
   int32_t v = 0;
   int64_t deg = 0;
   if (valid) {
     v = __ldg(p.out_idx + e);
-    claimed = ms_relax<W>(p, fu, v, nxt, touched);
+    claimed = ms_relax<W>(p, fu, u, v, nxt, touched);
     if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
   }
-  ms_enqueue(p, claimed, v, deg, next_parity, Rn, acc);
+  ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+}
+
+// Walks edge positions [x0, x1) of a big-vertex list (vertices q[cap-1-j],
+// prefix offsets boff[j], all of out-degree > 32).
+template <int W>
+__device__ void ms_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *nxt,
+                              uint32_t *touched, const int32_t *bq, int64_t cap,
+                              const uint32_t *boff, unsigned nbig, unsigned x0, unsigned x1,
+                              int32_t *q, uint32_t *qoff, MsRound *Rn, MsAcc &acc) {
+  const int lane = lane_id();
+  unsigned lo = 0, hi = nbig - 1;
+  while (lo < hi) {
+    const unsigned mid = (lo + hi + 1) >> 1;
+    if (boff[mid] <= x0)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  unsigned j = lo;
+  int32_t vj = bq[cap - 1 - (int64_t)j];
+  int64_t sj = __ldg(p.out_off + vj);
+  unsigned oj = boff[j];
+  unsigned endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
+  Mask<W> fj = ld_mask<W>(cur, vj);
+  for (unsigned base = x0; base < x1; base += 32) {
+    while (base >= endj) {
+      ++j;
+      vj = bq[cap - 1 - (int64_t)j];
+      sj = __ldg(p.out_off + vj);
+      oj = boff[j];
+      endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
+      fj = ld_mask<W>(cur, vj);
+    }
+    const unsigned x = base + lane;
+    const bool valid = x < x1;
+    int32_t u = vj;
+    int64_t e = sj + (int64_t)(x - oj);
+    Mask<W> fu = fj;
+    if (__ballot_sync(kMsFull, valid && x >= endj)) {
+      const int32_t vn = bq[cap - 1 - (int64_t)(j + 1)];
+      if (valid && x >= endj) {
+        u = vn;
+        e = __ldg(p.out_off + vn) + (int64_t)(x - endj);
+        fu = ld_mask<W>(cur, vn);
+      }
+    }
+    ms_push_step<W>(p, valid, fu, u, e, nxt, touched, q, qoff, Rn, acc);
+  }
 }
 
 template <int W>
@@ -425,66 +637,61 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
                         uint32_t *touched, MsRound *Rc, MsRound *Rn, MsAcc &acc) {
   __shared__ int32_t s_u[kMsBlock / 32][32];
   __shared__ int64_t s_s[kMsBlock / 32][32];
-  __shared__ int32_t s_x[kMsBlock / 32][32];
+  __shared__ int64_t s_x[kMsBlock / 32][32];
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
-  const int gw = warp_id_global();
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int parity = L & 1, next_parity = parity ^ 1;
-  const int32_t *q = parity ? p.queue1 : p.queue0;
-  const int32_t *h = parity ? p.heavy1 : p.heavy0;
+  const int32_t *qc = parity ? p.queue1 : p.queue0;
+  const uint32_t *bc = parity ? p.bigoff1 : p.bigoff0;
+  const int32_t *hc = parity ? p.hubq1 : p.hubq0;
+  const uint32_t *hbc = parity ? p.huboff1 : p.huboff0;
+  int32_t *qn = next_parity ? p.queue1 : p.queue0;
+  uint32_t *bn = next_parity ? p.bigoff1 : p.bigoff0;
 
-  const unsigned nheavy = *(volatile unsigned *)&Rc->nheavy;
-  for (unsigned b = 0; b < nheavy; ++b) {
-    const int32_t u = h[b];
-    const Mask<W> fu = ld_mask<W>(cur, u);
-    const int64_t s = __ldg(p.out_off + u), e = __ldg(p.out_off + u + 1);
-    for (int64_t base = s + (int64_t)gw * 32; base < e; base += (int64_t)nwarps * 32) {
-      const int64_t i = base + lane;
-      ms_push_step<W>(p, i < e, fu, i, nxt, touched, next_parity, Rn, acc);
-    }
-  }
-  const unsigned nmed = *(volatile unsigned *)&Rc->nmedium;
+  const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
+  const unsigned long long hubw = *(volatile unsigned long long *)&Rc->hub;
+  const unsigned nbig = (unsigned)(bigw >> 32), big_edges = (unsigned)bigw;
+  const unsigned nhubf = (unsigned)(hubw >> 32), hub_edges = (unsigned)hubw;
   const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
-  const unsigned nitems = nmed + (nlight + 31u) / 32u;
-  while (true) {
-    unsigned item = 0;
-    if (lane == 0) item = atomicAdd(&Rc->work, 1u);
-    item = __shfl_sync(kMsFull, item, 0);
-    if (item >= nitems) break;
-    if (item < nmed) {
-      const int32_t u = q[p.n - 1 - (int64_t)item];
-      const Mask<W> fu = ld_mask<W>(cur, u);
-      const int64_t s = __ldg(p.out_off + u), e = __ldg(p.out_off + u + 1);
-      for (int64_t base = s; base < e; base += 32) {
-        const int64_t i = base + lane;
-        ms_push_step<W>(p, i < e, fu, i, nxt, touched, next_parity, Rn, acc);
-      }
+  const unsigned nb = (big_edges + kPushChunk - 1) / kPushChunk;
+  const unsigned nh = (hub_edges + kPushChunk - 1) / kPushChunk;
+  const unsigned nitems = nb + nh + (nlight + 31u) / 32u;
+  unsigned item = (unsigned)warp_id_global();
+  while (item < nitems) {
+    if (item < nb) {
+      const unsigned x0 = item * kPushChunk;
+      ms_push_chunk<W>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0,
+                       min(x0 + (unsigned)kPushChunk, big_edges), qn, bn, Rn, acc);
+    } else if (item < nb + nh) {
+      const unsigned x0 = (item - nb) * kPushChunk;
+      ms_push_chunk<W>(p, cur, nxt, touched, hc, p.nhub, hbc, nhubf, x0,
+                       min(x0 + (unsigned)kPushChunk, hub_edges), qn, bn, Rn, acc);
     } else {
-      const unsigned idx = (item - nmed) * 32u + lane;
-      int32_t u = 0;
-      int64_t s = 0;
-      int d = 0;
+      const unsigned idx = (item - nb - nh) * 32u + lane;
+      int32_t u = -1;
+      int64_t s = 0, d = 0;
       if (idx < nlight) {
-        u = q[idx];
+        u = qc[idx];
         s = __ldg(p.out_off + u);
-        d = (int)(__ldg(p.out_off + u + 1) - s);
+        d = __ldg(p.out_off + u + 1) - s;
       }
-      int incl = d;
+      int64_t incl = d;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(kMsFull, incl, o);
+        const int64_t t = __shfl_up_sync(kMsFull, incl, o);
         if (lane >= o) incl += t;
       }
-      const int total = __shfl_sync(kMsFull, incl, 31);
+      const int64_t total = __shfl_sync(kMsFull, incl, 31);
       s_u[wib][lane] = u;
       s_s[wib][lane] = s;
       s_x[wib][lane] = incl - d;
       __syncwarp();
-      for (int base = 0; base < total; base += 32) {
-        const int t = base + lane;
+      for (int64_t base = 0; base < total; base += 32) {
+        const int64_t t = base + lane;
         const bool valid = t < total;
         int64_t e = 0;
+        int32_t uu = 0;
         Mask<W> fu = Mask<W>::zero();
         if (valid) {
           int lo = 0, hi = 31;
@@ -495,53 +702,54 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
             else
               hi = mid - 1;
           }
-          fu = ld_mask<W>(cur, s_u[wib][lo]);
+          uu = s_u[wib][lo];
+          fu = ld_mask<W>(cur, uu);
           e = s_s[wib][lo] + (t - s_x[wib][lo]);
         }
-        ms_push_step<W>(p, valid, fu, e, nxt, touched, next_parity, Rn, acc);
+        ms_push_step<W>(p, valid, fu, uu, e, nxt, touched, qn, bn, Rn, acc);
       }
       __syncwarp();
     }
+    unsigned nextitem = 0;
+    if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
+    item = __shfl_sync(kMsFull, nextitem, 0);
   }
 }
 
-// After a push round: for every newly reached vertex, merge its lanes into
-// vis and resolve each lane's parent by scanning the ascending in-list.
+// After a push round: every newly reached non-hub vertex merges its lanes
+// into vis and finds each lane's parent by scanning its ascending in-list
+// (it ends: every lane has a frontier source there).  Hubs are finalized from
+// their candidates.
 template <int W>
-__device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, const uint64_t *nxt,
-                           const MsRound *Rn, MsAcc &acc) {
+__device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
+                           MsRound *Rn, MsAcc &acc) {
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
   const int32_t *q = next_parity ? p.queue1 : p.queue0;
-  const int32_t *h = next_parity ? p.heavy1 : p.heavy0;
   const int64_t nl = *(volatile unsigned *)&Rn->nlight;
-  const int64_t nm = *(volatile unsigned *)&Rn->nmedium;
-  const int64_t nh = *(volatile unsigned *)&Rn->nheavy;
-  const int64_t total = nl + nm + nh;
+  const int64_t nbg = (int64_t)(*(volatile unsigned long long *)&Rn->big >> 32);
+  const int64_t total = nl + nbg;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total;
        base += nthreads) {
     const int64_t j = base + lane_id();
-    int64_t v = 0;
+    int64_t v = 0, s = 0, e = 0;
     Mask<W> nw = Mask<W>::zero();
     if (j < total) {
-      if (j < nl)
-        v = q[j];
-      else if (j < nl + nm)
-        v = q[p.n - 1 - (j - nl)];
-      else
-        v = h[j - nl - nm];
+      v = j < nl ? q[j] : q[p.n - 1 - (j - nl)];
       nw = ld_mask<W>(nxt, v);
       st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
       acc.visits += (unsigned long long)nw.popc();
       acc_lanes<W>(acc, nw);
+      s = __ldg(p.in_off + v);
+      e = __ldg(p.in_off + v + 1);
     }
-    // every lane of nw has a frontier source in v's in-list: the scan ends
-    scan_group<W>(p, v, nw, cur, L + 1);
+    scan_group<W>(p, v, s, e, nw, cur, L + 1);
   }
+  if (p.nhub > 0) hub_finalize<W>(p, L, nxt, Rn, acc);
 }
 
 template <int W>
-__global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
+__global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
   MsCtl *ctl = p.ctl;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
@@ -562,34 +770,35 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
   }
   bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
   // seed: lane i starts at roots[i] (block 0)
-  if (ok && blockIdx.x == 0) {
-    if (threadIdx.x < p.k) {
-      const int i = threadIdx.x;
-      const int32_t r = p.roots[i];
-      const unsigned long long bit = 1ull << (i & 63);
-      atomicOr(reinterpret_cast<unsigned long long *>(p.vis + (int64_t)r * W + (i >> 6)), bit);
-      atomicOr(reinterpret_cast<unsigned long long *>(p.fr0 + (int64_t)r * W + (i >> 6)), bit);
-      p.levels[(int64_t)i * p.n + r] = 0;
-      p.parents[(int64_t)i * p.n + r] = r;
-      bool first = true;
-      for (int j = 0; j < i; ++j) first = first && (p.roots[j] != r);
-      if (first) {
-        const int64_t deg = p.out_off[r + 1] - p.out_off[r];
-        MsRound *R0 = &ctl->rec[0];
-        if (deg <= kLightMax)
-          p.queue0[atomicAdd(&R0->nlight, 1u)] = r;
-        else if (deg <= kMediumMax)
-          p.queue0[p.n - 1 - (int64_t)atomicAdd(&R0->nmedium, 1u)] = r;
-        else
-          p.heavy0[atomicAdd(&R0->nheavy, 1u)] = r;
-        atomicAdd(&R0->nf, 1ull);
-        atomicAdd(&R0->mf, (unsigned long long)deg);
+  if (ok && blockIdx.x == 0 && threadIdx.x < p.k) {
+    const int i = threadIdx.x;
+    const int32_t r = p.roots[i];
+    const unsigned long long bit = 1ull << (i & 63);
+    atomicOr(reinterpret_cast<unsigned long long *>(p.vis + (int64_t)r * W + (i >> 6)), bit);
+    atomicOr(reinterpret_cast<unsigned long long *>(p.fr0 + (int64_t)r * W + (i >> 6)), bit);
+    p.levels[(int64_t)i * p.n + r] = 0;
+    p.parents[(int64_t)i * p.n + r] = r;
+    bool first = true;
+    for (int j = 0; j < i; ++j) first = first && (p.roots[j] != r);
+    if (first) {
+      const int64_t deg = p.out_off[r + 1] - p.out_off[r];
+      MsRound *R0 = &ctl->rec[0];
+      if (deg <= kLightMax) {
+        p.queue0[atomicAdd(&R0->nlight, 1u)] = r;
+      } else {
+        // roots are queued one by one: a 64-bit add keeps index and offset paired
+        const unsigned long long old =
+            atomicAdd(&R0->big, (1ull << 32) | (unsigned long long)deg);
+        p.queue0[p.n - 1 - (int64_t)(old >> 32)] = r;
+        p.bigoff0[old >> 32] = (unsigned)old;
       }
-      if (i == 0) {
-        const Mask<W> a0 = lane_mask<W>(p.k);
-        ctl->rec[0].lanes[0] = a0.w[0];
-        ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
-      }
+      atomicAdd(&R0->nf[0], 1ull);
+      atomicAdd(&R0->mf[0], (unsigned long long)deg);
+    }
+    if (i == 0) {
+      const Mask<W> a0 = lane_mask<W>(p.k);
+      ctl->rec[0].lanes[0] = a0.w[0];
+      ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
     }
   }
   if (ok) ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
@@ -617,8 +826,9 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
     // longer read by anyone; the record is next appended to in round L + 2
     if (leader) {
       MsRound *Rz = &ctl->rec[(L + 3) % kRing];
-      Rz->nf = Rz->visits = Rz->mf = 0;
-      Rz->nlight = Rz->nmedium = Rz->nheavy = Rz->work = 0;
+      for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->visits[i] = Rz->mf[i] = 0;
+      Rz->big = Rz->hub = 0;
+      Rz->nlight = Rz->work = 0;
       Rz->lanes[0] = Rz->lanes[1] = 0;
     }
     for (int64_t i = gtid; i < p.n * W; i += nthreads) old[i] = 0;
@@ -628,18 +838,19 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
 #pragma unroll
       for (int i = 0; i < W; ++i) active.w[i] = *(volatile unsigned long long *)&Rc->lanes[i];
       ms_pull<W>(p, L, cur, nxt, active, Rn, acc);
-      ms_flush(acc, Rn);
-      if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
+      if (p.nhub > 0) {
+        if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
+        hub_finalize<W>(p, L, nxt, Rn, acc);
+      }
     } else {
       ms_push<W>(p, L, cur, nxt, touched, Rc, Rn, acc);
       if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
       ms_resolve<W>(p, L, cur, nxt, Rn, acc);
-      ms_flush(acc, Rn);
-      if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
     }
-    const unsigned long long nf = *(volatile unsigned long long *)&Rn->nf;
-    const unsigned long long visits = *(volatile unsigned long long *)&Rn->visits;
-    const unsigned long long mf = *(volatile unsigned long long *)&Rn->mf;
+    ms_flush(acc, Rn);
+    if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
+    unsigned long long nf, visits, mf;
+    ms_read_counters(Rn, nf, visits, mf);
     if (leader && L < CG_HISTORY) {
       p.stats->nf_history[L] = (int64_t)visits;
       p.stats->direction_history[L] = dir;
@@ -698,25 +909,66 @@ __global__ void __launch_bounds__(kMsBlock) msbfs_persistent(MsParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// per-graph hub list: vertices of in-degree > kHubDeg, their chunk prefix
+__global__ void hub_mark_kernel(int64_t n, const int64_t *__restrict__ in_off, int32_t *hub_slot,
+                                int32_t *hub_vtx, unsigned *count) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = in_off[v + 1] - in_off[v];
+    int32_t slot = -1;
+    if (d > kHubDeg) {
+      slot = (int32_t)atomicAdd(count, 1u);
+      hub_vtx[slot] = (int32_t)v;
+    }
+    hub_slot[v] = slot;
+  }
+}
+
+__global__ void hub_chunks_kernel(int nhub, const int64_t *__restrict__ in_off,
+                                  const int32_t *__restrict__ hub_vtx, uint32_t *chunks) {
+  for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < nhub; h += gridDim.x * blockDim.x) {
+    const int32_t v = hub_vtx[h];
+    chunks[h] = (uint32_t)((in_off[v + 1] - in_off[v] + kHubChunk - 1) / kHubChunk);
+  }
+}
+
 struct MsState {
-  uint64_t *bits;
-  uint32_t *touched;
-  int32_t *queue;
-  int32_t *heavy;
-  MsCtl *ctl;
-  int64_t hcap;
+  uint64_t *bits = nullptr;
+  uint32_t *touched = nullptr;
+  int32_t *queue = nullptr;
+  uint32_t *bigoff = nullptr;
+  int32_t *hubq = nullptr;
+  uint32_t *huboff = nullptr;
+  int32_t *hub_slot = nullptr;
+  int32_t *hub_vtx = nullptr;
+  uint32_t *hub_choff = nullptr;
+  uint32_t *hub_cand = nullptr;
+  uint64_t *hub_found = nullptr;
+  MsCtl *ctl = nullptr;
+  int64_t bcap = 0;
+  int nhub = 0;
+  int lane_words = 0;
 };
 
+static void ms_free_state(MsState *s) {
+  if (!s) return;
+  cudaFree(s->bits);
+  cudaFree(s->touched);
+  cudaFree(s->queue);
+  cudaFree(s->bigoff);
+  cudaFree(s->hubq);
+  cudaFree(s->huboff);
+  cudaFree(s->hub_slot);
+  cudaFree(s->hub_vtx);
+  cudaFree(s->hub_choff);
+  cudaFree(s->hub_cand);
+  cudaFree(s->hub_found);
+  cudaFree(s->ctl);
+  delete s;
+}
+
 void msbfs_release(cg_graph *g) {
-  MsState *s = reinterpret_cast<MsState *>(g->ms_ctl);
-  if (s) {
-    cudaFree(s->bits);
-    cudaFree(s->touched);
-    cudaFree(s->queue);
-    cudaFree(s->heavy);
-    cudaFree(s->ctl);
-    delete s;
-  }
+  ms_free_state(reinterpret_cast<MsState *>(g->ms_ctl));
   g->ms_ctl = nullptr;
   cudaFree(g->ms_levels);
   cudaFree(g->ms_parents);
@@ -725,36 +977,94 @@ void msbfs_release(cg_graph *g) {
   g->ms_lane_words = 0;
 }
 
+int64_t bfs_big_capacity(int64_t n, int64_t nnz);
+
+static int ms_build_hubs(cg_graph *g, MsState *s) {
+  const int64_t cap = g->nnz / (kHubDeg + 1) + 1;
+  unsigned *d_count = nullptr;
+  if (cudaMalloc(&s->hub_slot, sizeof(int32_t) * (size_t)g->n) != cudaSuccess ||
+      cudaMalloc(&s->hub_vtx, sizeof(int32_t) * (size_t)cap) != cudaSuccess ||
+      cudaMalloc(&d_count, sizeof(unsigned)) != cudaSuccess) {
+    cudaFree(d_count);
+    return CG_ERR_OUT_OF_MEMORY;
+  }
+  int rc = CG_OK;
+  do {
+    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned), g->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "hub count"); break; }
+    int blocks = (int)((g->n + 255) / 256);
+    if (blocks > g->num_sms * 16) blocks = g->num_sms * 16;
+    hub_mark_kernel<<<blocks, 256, 0, g->stream>>>(g->n, g->in_off, s->hub_slot, s->hub_vtx,
+                                                    d_count);
+    unsigned nhub = 0;
+    e = cudaMemcpyAsync(&nhub, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "hub mark"); break; }
+    s->nhub = (int)nhub;
+    const size_t nh = nhub > 0 ? nhub : 1;
+    if (cudaMalloc(&s->hub_choff, sizeof(uint32_t) * (nh + 1)) != cudaSuccess ||
+        cudaMalloc(&s->hub_cand, sizeof(uint32_t) * nh * 64 * s->lane_words) != cudaSuccess ||
+        cudaMalloc(&s->hub_found, sizeof(uint64_t) * nh * s->lane_words) != cudaSuccess ||
+        cudaMalloc(&s->hubq, sizeof(int32_t) * 2 * nh) != cudaSuccess ||
+        cudaMalloc(&s->huboff, sizeof(uint32_t) * 2 * nh) != cudaSuccess) {
+      rc = CG_ERR_OUT_OF_MEMORY;
+      break;
+    }
+    uint32_t *chunks = nullptr;
+    if (cudaMalloc(&chunks, sizeof(uint32_t) * nh) != cudaSuccess) {
+      rc = CG_ERR_OUT_OF_MEMORY;
+      break;
+    }
+    if (nhub) hub_chunks_kernel<<<(nhub + 255) / 256, 256, 0, g->stream>>>(nhub, g->in_off,
+                                                                          s->hub_vtx, chunks);
+    uint32_t *h_chunks = new uint32_t[nh + 1];
+    h_chunks[0] = 0;
+    e = cudaMemcpyAsync(h_chunks + 1, chunks, sizeof(uint32_t) * nhub, cudaMemcpyDeviceToHost,
+                        g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e == cudaSuccess) {
+      for (unsigned h = 0; h < nhub; ++h) h_chunks[h + 1] += h_chunks[h];
+      e = cudaMemcpyAsync(s->hub_choff, h_chunks, sizeof(uint32_t) * (nhub + 1),
+                          cudaMemcpyHostToDevice, g->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    }
+    delete[] h_chunks;
+    cudaFree(chunks);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "hub chunks"); break; }
+    g->device_bytes += sizeof(int32_t) * g->n + sizeof(int32_t) * cap +
+                       nh * (sizeof(uint32_t) * (1 + 64 * s->lane_words + 4) +
+                             sizeof(uint64_t) * s->lane_words);
+  } while (0);
+  cudaFree(d_count);
+  return rc;
+}
+
 static int ms_alloc_state(cg_graph *g, int lane_words) {
   if (g->ms_ctl && g->ms_lane_words == lane_words) return CG_OK;
-  if (g->ms_ctl) {
-    MsState *s = reinterpret_cast<MsState *>(g->ms_ctl);
-    cudaFree(s->bits);
-    cudaFree(s->touched);
-    cudaFree(s->queue);
-    cudaFree(s->heavy);
-    cudaFree(s->ctl);
-    delete s;
-    g->ms_ctl = nullptr;
-  }
+  ms_free_state(reinterpret_cast<MsState *>(g->ms_ctl));
+  g->ms_ctl = nullptr;
   MsState *s = new MsState();
-  s->hcap = g->nnz / (kMediumMax + 1) + 1;
-  if (s->hcap > g->n) s->hcap = g->n;
+  s->lane_words = lane_words;
+  s->bcap = bfs_big_capacity(g->n, g->nnz);
   const size_t bits = sizeof(uint64_t) * 4 * (size_t)g->n * lane_words;
   const size_t words = (size_t)((g->n + 31) / 32);
   if (cudaMalloc(&s->bits, bits) != cudaSuccess ||
       cudaMalloc(&s->touched, sizeof(uint32_t) * 2 * words) != cudaSuccess ||
       cudaMalloc(&s->queue, sizeof(int32_t) * 2 * (size_t)g->n) != cudaSuccess ||
-      cudaMalloc(&s->heavy, sizeof(int32_t) * 2 * (size_t)s->hcap) != cudaSuccess ||
+      cudaMalloc(&s->bigoff, sizeof(uint32_t) * 2 * (size_t)s->bcap) != cudaSuccess ||
       cudaMalloc(&s->ctl, sizeof(MsCtl)) != cudaSuccess) {
-    g->ms_ctl = s;
-    msbfs_release(g);
+    ms_free_state(s);
     return CG_ERR_OUT_OF_MEMORY;
+  }
+  int rc = ms_build_hubs(g, s);
+  if (rc) {
+    ms_free_state(s);
+    return rc;
   }
   g->ms_ctl = s;
   g->ms_lane_words = lane_words;
   g->device_bytes += bits + sizeof(uint32_t) * 2 * words + sizeof(int32_t) * 2 * g->n +
-                     sizeof(int32_t) * 2 * s->hcap + sizeof(MsCtl);
+                     sizeof(uint32_t) * 2 * s->bcap + sizeof(MsCtl);
   return CG_OK;
 }
 
@@ -806,8 +1116,19 @@ static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
   p.touched1 = s->touched + p.words;
   p.queue0 = s->queue;
   p.queue1 = s->queue + g->n;
-  p.heavy0 = s->heavy;
-  p.heavy1 = s->heavy + s->hcap;
+  p.bigoff0 = s->bigoff;
+  p.bigoff1 = s->bigoff + s->bcap;
+  const int64_t nh = s->nhub > 0 ? s->nhub : 1;
+  p.hubq0 = s->hubq;
+  p.hubq1 = s->hubq + nh;
+  p.huboff0 = s->huboff;
+  p.huboff1 = s->huboff + nh;
+  p.hub_slot = s->hub_slot;
+  p.hub_vtx = s->hub_vtx;
+  p.hub_choff = s->hub_choff;
+  p.hub_cand = s->hub_cand;
+  p.hub_found = s->hub_found;
+  p.nhub = s->nhub;
   p.levels = d_levels;
   p.parents = d_parents;
   p.ctl = s->ctl;
@@ -820,6 +1141,9 @@ static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
   p.timeout_ns = (long long)(g->opt.wait_timeout_ms > 0 ? g->opt.wait_timeout_ms : 1000) * 1000000ll;
   for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = i < k ? (int32_t)roots[i] : 0;
   CG_CUDA(cudaMemsetAsync(s->ctl, 0, sizeof(MsCtl), g->stream));
+  // candidates start at "none"; a pass cut short by an error leaves them dirty
+  CG_CUDA(cudaMemsetAsync(s->hub_cand, 0xff, sizeof(uint32_t) * (size_t)nh * 64 * W, g->stream));
+  CG_CUDA(cudaMemsetAsync(s->hub_found, 0, sizeof(uint64_t) * (size_t)nh * W, g->stream));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(per_sm * g->num_sms);
   cfg.blockDim = dim3(block);
