@@ -54,6 +54,15 @@ def parse():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--no-batched", action="store_true",
                   help="skip the multi-source (bit-lane) measurement")
+  ap.add_argument("--workload", default="graph500", choices=["graph500", "uneven", "serving"],
+                  help="graph500: per-root + batched on one R-MAT graph (default); uneven: "
+                       "256 roots in 128-lane batches over R-MAT s22 e32, directed ER 2^22 "
+                       "and the 4096^2 grid, autotuned; serving: Poisson query sweep over "
+                       "resident R-MAT s20/s22/s24/s26")
+  ap.add_argument("--serving-scales", default="20,22,24,26")
+  ap.add_argument("--serving-rates", default="100,1000,10000,100000")
+  ap.add_argument("--serving-seconds", type=float, default=2.0,
+                  help="arrival window per rate (query count capped at 4000)")
   return ap.parse_args()
 
 
@@ -128,6 +137,18 @@ def make_graph(args):
   t0 = time.perf_counter()
   a = generators.rmat(args.scale, args.edgefactor, args.seed)
   return a, time.perf_counter() - t0
+
+
+def make_graph_device(args):
+  """The same R-MAT graph drawn and built on the GPU (bit-identical to the
+  host generator); returns (Graph, GraphArrays, seconds)."""
+  import torch
+  from ceregraphs_gb300 import generators
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  g, a = generators.rmat_device(args.scale, args.edgefactor, args.seed)
+  torch.cuda.synchronize()
+  return g, a, time.perf_counter() - t0
 
 
 def workload_config(args, a, extra=None):
@@ -250,16 +271,9 @@ def run_ours(args):
   from ceregraphs_gb300.engine import Graph, PinnedBuffer
   from ceregraphs_gb300.graph500 import EdgeCounter, pick_sources
 
-  a, gen_s = make_graph(args)
+  g, a, gen_s = make_graph_device(args)
   roots_all = pick_sources(a, args.roots, args.root_seed)
   roots = roots_all  # every replica runs the full root set (weak scaling)
-  counter = EdgeCounter(a)
-  deg = np.diff(a.in_off if a.symmetric else a.out_off)
-
-  t0 = time.perf_counter()
-  g = Graph(a)
-  torch.cuda.synchronize()
-  construct_s = time.perf_counter() - t0
   dirmap = {"auto": _lib.CG_DIR_AUTO, "topdown": _lib.CG_DIR_TOPDOWN,
             "bottomup": _lib.CG_DIR_BOTTOMUP, "tau": _lib.CG_DIR_TAU}
   g.set_options(direction=dirmap[args.direction])
@@ -271,17 +285,20 @@ def run_ours(args):
   torch.cuda.synchronize()
   stream = torch.cuda.ExternalStream(g.stream)
 
-  # m per root (device count, checked once against the host rule below)
+  # m per root (device count; checked against the host rule on smaller graphs)
   for i, r in enumerate(roots):
     g.bfs_device(r, d_lv[i], d_pa[i])
   st = g.last_stats()
   if st["status"] != 0:
     raise RuntimeError(f"search failed: {st}")
   m = g.count_edges(d_lv, k)
-  lv_host = d_lv.cpu().numpy()
-  m_host = np.array([counter.m(lv_host[i] >= 0) for i in range(k)])
-  assert np.array_equal(m, m_host), "device and host edge counts differ"
-  nnz_vis = np.array([int(deg[lv_host[i] >= 0].sum()) for i in range(k)])
+  if a.nnz <= 100_000_000:
+    counter = EdgeCounter(a)
+    lv_host = d_lv.cpu().numpy()
+    m_host = np.array([counter.m(lv_host[i] >= 0) for i in range(k)])
+    assert np.array_equal(m, m_host), "device and host edge counts differ"
+  deg_t = torch.from_numpy(np.diff(a.out_lists()[0])).cuda()
+  nnz_vis = np.array([int(((d_lv[i] >= 0).to(torch.int64) * deg_t).sum()) for i in range(k)])
   alg_bytes = 4 * nnz_vis + 8 * (n + 1) + 8 * n   # B_1 per search
 
   def one_step(ev):
@@ -386,8 +403,7 @@ def run_ours(args):
       "warmup": max(args.warmup, 3), "ms_per_step": step_ms, "higher_is_better": True,
       "scaling": "weak", "vs_baseline": None, "dtype": "int32",
       "data": "synthetic (RMAT, the reference generator's recipe, bit-identical)",
-      "config": workload_config(args, a, {"construction_s": round(construct_s, 4),
-                                          "generation_s": round(gen_s, 2)}),
+      "config": workload_config(args, a, {"generation_and_construction_s": round(gen_s, 3)}),
       "e2e": {"value": e2e_value * world, "unit": "GTEPS", "h2d_bytes_per_step": 8 * k,
               "d2h_bytes_per_step": 4 * n * k,
               "note": "cg_bfs: launch + all rounds + parents copied to page-locked host memory"},
@@ -423,10 +439,137 @@ def run_ours(args):
   return 0
 
 
+def run_uneven(args):
+  """Three graphs of uneven depth, 256 roots each (seed 5) in batches of 128
+  lanes, knobs chosen per graph by the autotuner; every lane of a sampled batch
+  is checked against single-root searches."""
+  import torch
+  from ceregraphs_gb300 import autotune, generators
+  from ceregraphs_gb300.bfs_timing import harmonic_mean
+  from ceregraphs_gb300.engine import Graph
+  from ceregraphs_gb300.graph500 import pick_sources
+  torch.cuda.set_device(0)
+  specs = [("rmat22-e32", lambda: generators.rmat_device(22, 32, 0)),
+           ("er22-d8-directed", lambda: generators.er_directed_device(22, 8, 4)),
+           ("grid4096", lambda: (lambda a: (Graph(a), a))(generators.grid2d(4096)))]
+  out = {}
+  tot_m = tot_s = 0.0
+  for name, make in specs:
+    t0 = time.perf_counter()
+    g, a = make()
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    roots = pick_sources(a, 256, 5)
+    k = len(roots)
+    tune = autotune.tune(g, a, roots[:128], mode="batched",
+                         space={"lane_words": [1, 2], "ms_alpha": [1.0, 4.0, 16.0],
+                                "block_size": [512]}, reps=1, cache=autotune.Cache(
+                                    os.path.join(HERE, "_work", "tune_cache.json")))
+    lanes = 64 * g.options().lane_words
+    d_lv = torch.empty((k, a.n), dtype=torch.int32, device="cuda")
+    d_pa = torch.empty((k, a.n), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(g.stream)
+    g.msbfs_device(roots, d_lv, d_pa)
+    g.last_stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+      g.msbfs_device(roots, d_lv, d_pa)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    st = g.last_stats()
+    batch_ms = e0.elapsed_time(e1) / args.steps
+    m = g.count_edges(d_lv, k)
+    # per-root sample: 8 roots, direction-optimizing single searches
+    sample = roots[:8]
+    lv1 = torch.empty(a.n, dtype=torch.int32, device="cuda")
+    pa1 = torch.empty(a.n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    per_ms, same = [], True
+    for i, r in enumerate(sample):
+      g.bfs_device(r, lv1, pa1)
+      g.last_stats()
+      t0 = time.perf_counter()
+      g.bfs_device(r, lv1, pa1)
+      g.last_stats()
+      per_ms.append((time.perf_counter() - t0) * 1e3)
+      same = same and bool(torch.equal(lv1, d_lv[i]) and torch.equal(pa1, d_pa[i]))
+    per_gteps = [float(m[i]) / (per_ms[i] * 1e-3) / 1e9 for i in range(len(sample))]
+    out[name] = {"n": a.n, "nnz": a.nnz, "symmetric": a.symmetric, "roots": k,
+                 "generation_s": round(gen_s, 2), "lanes": lanes,
+                 "tuned": tune["options"], "batch_ms_all_roots": batch_ms,
+                 "batched_gteps": float(m.sum()) / (batch_ms * 1e-3) / 1e9,
+                 "per_root_sample_hm_gteps": harmonic_mean(per_gteps),
+                 "rounds_max": st["rounds"], "bit_exact_sample": same}
+    tot_m += float(m.sum())
+    tot_s += batch_ms * 1e-3
+    g.close()
+    del d_lv, d_pa
+    torch.cuda.empty_cache()
+  line = {"metric": "batched GTEPS, 256 roots per graph in 64/128-lane batches (autotuned)",
+          "value": tot_m / tot_s / 1e9, "unit": "GTEPS", "n_gpus": 1, "steps": args.steps,
+          "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+          "dtype": "int32", "data": "synthetic (R-MAT reference recipe, ER, grid)",
+          "config": {"workload": "uneven-depth batching: rmat22-e32, er22-d8 directed, "
+                                 "grid 4096x4096; roots seed 5"},
+          "graphs": out}
+  print(json.dumps(line), flush=True)
+  return 0
+
+
+def run_serving(args):
+  """Continuous batching over resident R-MAT graphs with Poisson arrivals."""
+  import torch
+  from ceregraphs_gb300 import generators, serving
+  torch.cuda.set_device(0)
+  graphs, roots, info = {}, {}, {}
+  for sc in [int(x) for x in args.serving_scales.split(",")]:
+    t0 = time.perf_counter()
+    g, _ = generators.rmat_device(sc, 16, 0, export=False)
+    off = g.export_offsets()
+    torch.cuda.synchronize()
+    cand = np.nonzero(np.diff(off) > 0)[0]
+    name = f"rmat{sc}"
+    graphs[name] = g
+    roots[name] = cand
+    info[name] = {"n": g.n, "nnz": g.nnz, "build_s": round(time.perf_counter() - t0, 2)}
+    del off
+  torch.cuda.empty_cache()
+  budget = 96 << 30
+  rows = []
+  best = 0.0
+  for rate in [float(x) for x in args.serving_rates.split(",")]:
+    count = int(min(4000, max(100, rate * args.serving_seconds)))
+    arrivals = serving.poisson_arrivals(rate, count, roots, seed=6)
+    srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget)
+    rep = srv.run(arrivals, realtime=True).summary()
+    srv.close()
+    base = serving.serial_baseline(graphs, arrivals, realtime=True).summary()
+    rows.append({"rate_qps": rate, "queries": count, "batched": rep, "serial": base})
+    best = max(best, rep["throughput_qps"])
+  line = {"metric": "queries/s and p50/p99 query ms, continuous batching vs serial per-query BFS",
+          "value": best, "unit": "queries/s", "n_gpus": 1, "steps": len(rows), "warmup": 0,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+          "data": "synthetic (R-MAT reference recipe), Poisson arrivals seed 6",
+          "config": {"workload": "serving over resident rmat " + args.serving_scales +
+                                 ", edgefactor 16, uniform non-isolated roots",
+                     "graphs": info, "hbm_budget_bytes": budget, "lanes_per_graph": 64},
+          "rates": rows}
+  print(json.dumps(line), flush=True)
+  for g in graphs.values():
+    g.close()
+  return 0
+
+
 def main():
   args = parse()
   if args.impl == "reference":
     return run_reference(args)
+  if args.workload == "uneven":
+    return run_uneven(args)
+  if args.workload == "serving":
+    return run_serving(args)
   return run_ours(args)
 
 

@@ -104,6 +104,14 @@ SIGNATURES = {
     "cg_graph_export": ([_P, _P, _P, _P, _P], ctypes.c_int),
     "cg_bfs_noalloc": ([ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, ctypes.c_int64, _P, _P,
                         ctypes.POINTER(CgStats), _P], ctypes.c_int),
+    "cg_pool_create": ([_P, ctypes.c_int32, ctypes.POINTER(_P)], ctypes.c_int),
+    "cg_pool_destroy": ([_P], ctypes.c_int),
+    "cg_pool_admit": ([_P, ctypes.c_int64, _P, _P, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+    "cg_pool_step": ([_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64),
+                      ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+    "cg_pool_release": ([_P, ctypes.c_int32], ctypes.c_int),
+    "cg_pool_info": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)],
+                     ctypes.c_int),
     "cg_capture_begin": ([_P], ctypes.c_int),
     "cg_capture_end": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
     "cg_exec_launch": ([_P], ctypes.c_int),

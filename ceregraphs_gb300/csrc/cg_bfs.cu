@@ -281,15 +281,23 @@ __device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nx
     if (active) {
       s = __ldg(p.in_off + v);
       e = __ldg(p.in_off + v + 1);
-      const int64_t lim = min(e, s + (int64_t)kPullThreadScan);
-      for (int64_t i = s; i < lim; ++i) {
-        const int32_t u = __ldg(p.in_idx + i);
-        if ((cur[(uint32_t)u >> 5] >> (u & 31)) & 1u) {
-          p.parents[v] = u;
-          p.levels[v] = L + 1;
-          found = true;
-          break;
-        }
+      // the first kPullThreadScan sources: all loads issued before any test
+      int32_t u[kPullThreadScan];
+      uint32_t hit = 0;
+#pragma unroll
+      for (int k = 0; k < kPullThreadScan; ++k) u[k] = s + k < e ? __ldg(p.in_idx + s + k) : -1;
+#pragma unroll
+      for (int k = 0; k < kPullThreadScan; ++k)
+        if (u[k] >= 0 && ((cur[(uint32_t)u[k] >> 5] >> (u[k] & 31)) & 1u)) hit |= 1u << k;
+      if (hit) {
+        const int k = __ffs(hit) - 1;  // ascending list: the lowest hit is the minimum
+        int32_t uk = u[0];
+#pragma unroll
+        for (int t = 1; t < kPullThreadScan; ++t)
+          if (t == k) uk = u[t];
+        p.parents[v] = uk;
+        p.levels[v] = L + 1;
+        found = true;
       }
     }
     unsigned rest = __ballot_sync(kFull, active && !found && e > s + kPullThreadScan);
@@ -332,57 +340,31 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
   return x;
 }
 
-// Adds the block's per-thread counters into round record Rn (one atomic per
-// counter per block, skipped when zero).
-__device__ void flush_acc(Acc &acc, RoundRec *Rn) {
+// Block totals of the per-thread counters (all threads call; thread 0 gets
+// the sums) -- the one __syncthreads of a round's end before the wait.
+__device__ void block_totals(Acc &acc, unsigned long long &a, unsigned long long &b,
+                             unsigned long long &c) {
   __shared__ unsigned long long s_red[3][kBfsBlock / 32];
   const int lane = lane_id(), wib = threadIdx.x >> 5;
-  unsigned long long a = warp_sum(acc.nf), b = warp_sum(acc.mf), c = warp_sum(acc.visdeg);
+  a = warp_sum(acc.nf);
+  b = warp_sum(acc.mf);
+  c = warp_sum(acc.visdeg);
   if (lane == 0) {
     s_red[0][wib] = a;
     s_red[1][wib] = b;
     s_red[2][wib] = c;
   }
   __syncthreads();
-  if (wib == 0) {
+  if (threadIdx.x == 0) {
     const int nw = blockDim.x >> 5;
-    a = lane < nw ? s_red[0][lane] : 0ull;
-    b = lane < nw ? s_red[1][lane] : 0ull;
-    c = lane < nw ? s_red[2][lane] : 0ull;
-    a = warp_sum(a);
-    b = warp_sum(b);
-    c = warp_sum(c);
-    if (lane == 0) {
-      const int sh = blockIdx.x % kCounterShards;
-      if (a) atomicAdd(&Rn->nf[sh], a);
-      if (b) atomicAdd(&Rn->mf[sh], b);
-      if (c) atomicAdd(&Rn->visdeg[sh], c);
+    a = b = c = 0;
+    for (int i = 0; i < nw; ++i) {
+      a += s_red[0][i];
+      b += s_red[1][i];
+      c += s_red[2][i];
     }
   }
   acc = Acc();
-}
-
-// Totals of the sharded round counters, read after a grid-wide wait (all
-// threads of the block call; the result is the same in every block).
-__device__ void read_counters(const RoundRec *R, unsigned long long &nf, unsigned long long &mf,
-                              unsigned long long &vd) {
-  __shared__ unsigned long long s_tot[3];
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    const int which = lane / kCounterShards, sh = lane % kCounterShards;
-    unsigned long long x = 0;
-    if (which == 0) x = *(volatile const unsigned long long *)&R->nf[sh];
-    else if (which == 1) x = *(volatile const unsigned long long *)&R->mf[sh];
-    else if (which == 2) x = *(volatile const unsigned long long *)&R->visdeg[sh];
-#pragma unroll
-    for (int o = kCounterShards / 2; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-    if (sh == 0 && which < 3) s_tot[which] = x;
-  }
-  __syncthreads();
-  nf = s_tot[0];
-  mf = s_tot[1];
-  vd = s_tot[2];
-  __syncthreads();
 }
 
 __device__ __forceinline__ int next_direction(const BfsParams &p, int dir, unsigned long long nf,
@@ -408,16 +390,87 @@ __device__ __forceinline__ int next_direction(const BfsParams &p, int dir, unsig
   }
 }
 
-__global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
+// Payload of a round's grid-wide wait.
+constexpr unsigned kDone = 1u, kNextPull = 2u;
+
+// End of round L, run by the block that arrives last (it sees every block's
+// counters): the termination test of bool_pe.csl:1048-1100 (nf == 0 ends the
+// search), the direction for round L + 1, the statistics, and the reset of
+// the round record that round L + 1 accumulates into next.
+__device__ unsigned decide_round(const BfsParams &p, int L, int dir) {
+  BfsCtl *ctl = p.ctl;
+  const RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
+  unsigned long long nf = 0, mf = 0, vd = 0;
+#pragma unroll
+  for (int i = 0; i < kCounterShards; ++i) {
+    nf += *(volatile const unsigned long long *)&Rn->nf[i];
+    mf += *(volatile const unsigned long long *)&Rn->mf[i];
+    vd += *(volatile const unsigned long long *)&Rn->visdeg[i];
+  }
+  cg_stats *st = p.stats;
+  const long long now = global_ns();
+  if (L < CG_HISTORY) {
+    st->nf_history[L] = (int64_t)nf;
+    st->direction_history[L] = dir;
+    st->round_ns[L] = now - ctl->t_round;
+  }
+  ctl->t_round = now;
+  if (dir == kPull) ctl->pull_rounds += 1;
+  ctl->visited += nf;
+  bool done = nf == 0;
+  if (!done && L + 1 >= p.level_cap) {
+    atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
+    done = true;
+  }
+  const int next = next_direction(p, dir, nf, ctl->prev_nf, mf, ctl->explored);
+  ctl->explored += vd;
+  ctl->prev_nf = nf;
+  if (!done && next != dir) ctl->switches += 1;
+  RoundRec *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
+  for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->mf[i] = Rz->visdeg[i] = 0;
+  Rz->big = 0;
+  Rz->nlight = Rz->work = 0;
+  if (done) {
+    const int rounds = L + 1;
+    st->status = *(volatile int *)&ctl->status;
+    st->rounds = rounds;
+    st->visited = (int64_t)ctl->visited;
+    st->pull_rounds = ctl->pull_rounds;
+    st->switches = ctl->switches;
+    st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
+    st->finish_ns = 0;
+    st->device_ms = 0.f;
+  }
+  return (done ? kDone : 0u) | (next == kPull ? kNextPull : 0u);
+}
+
+struct RoundDecision {
+  const BfsParams *p;
+  int L, dir;
+  __device__ unsigned operator()() const { return decide_round(*p, L, dir); }
+};
+
+struct SetupDecision {
+  BfsCtl *ctl;
+  cg_stats *st;
+  __device__ unsigned operator()() const {
+    const long long now = global_ns();
+    st->setup_ns = now - ctl->t_start;
+    ctl->t_round = now;
+    return 0u;
+  }
+};
+
+__global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
+  __shared__ unsigned s_payload;
   BfsCtl *ctl = p.ctl;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int32_t root = (int32_t)p.root;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
-  const long long t_start = leader ? global_ns() : 0;
-  uint32_t *fr[3] = {p.fr0, p.fr1, p.fr2};
 
   // ---- phase 0: start_spmv -- reset outputs and bitmaps, seed the root ----
+  if (leader) ctl->t_start = global_ns();
   for (int64_t i = gtid; i < p.n; i += nthreads) {
     p.levels[i] = (i == root) ? 0 : -1;
     p.parents[i] = (i == root) ? root : -1;
@@ -434,6 +487,9 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
     R0->nf[0] = 1;
     R0->mf[0] = deg;
     R0->visdeg[0] = deg;
+    ctl->visited = 1;
+    ctl->prev_nf = 1;
+    ctl->explored = (unsigned long long)deg;
     if (deg <= kLightMax) {
       p.queue0[0] = root;
       R0->nlight = 1;
@@ -443,34 +499,24 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
       R0->big = (1ull << 32) | (unsigned long long)deg;
     }
   }
-  bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns, p.unmatched_wait ? 1u : 0u);
+  __syncthreads();
+  if (threadIdx.x == 0)
+    s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns,
+                                p.unmatched_wait ? 1u : 0u, SetupDecision{ctl, p.stats});
+  __syncthreads();
+  bool ok = s_payload != kWaitFailed;
 
+  uint32_t *fr0 = p.fr0, *fr1 = p.fr1, *fr2 = p.fr2;
   int dir = kPush;
   bool queued = true;  // F_L is in a queue (a pull round leaves it in the bitmap only)
   int L = 0;
-  int pull_rounds = 0, switches = 0;
-  unsigned long long prev_nf = 1, visited = 1;
-  unsigned long long explored = (unsigned long long)(p.out_off[root + 1] - p.out_off[root]);
   Acc acc;
-  long long t_round = leader ? global_ns() : 0;
-  if (leader) p.stats->setup_ns = t_round - t_start;
   while (ok) {
     RoundRec *Rc = &ctl->rec[L % kRing];
     RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
-    const uint32_t *cur = fr[L % 3];
-    uint32_t *nxt = fr[(L + 1) % 3];
-    uint32_t *old = fr[(L + 2) % 3];
-    if (leader) {
-      if (L > 0 && L - 1 < CG_HISTORY) {
-        const long long now = global_ns();
-        p.stats->round_ns[L - 1] = now - t_round;
-        t_round = now;
-      }
-      RoundRec *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
-      for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->mf[i] = Rz->visdeg[i] = 0;
-      Rz->big = 0;
-      Rz->nlight = Rz->work = 0;
-    }
+    const uint32_t *cur = fr0;  // F_L
+    uint32_t *nxt = fr1;        // F_{L+1}
+    uint32_t *old = fr2;        // F_{L-1}
     if (dir == kPush) {
       if (queued)
         push_round_queue(p, cur, nxt, L, Rc, Rn, acc);
@@ -486,47 +532,28 @@ __global__ void __launch_bounds__(kBfsBlock) bfs_persistent(BfsParams p) {
       if (c) p.vis[w] |= c;
       old[w] = 0;
     }
-    flush_acc(acc, Rn);
-    if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
-
-    unsigned long long nf, mf, vd;
-    read_counters(Rn, nf, mf, vd);
-    if (leader && L < CG_HISTORY) {
-      p.stats->nf_history[L] = (int64_t)nf;
-      p.stats->direction_history[L] = dir;
+    unsigned long long a, b, c;
+    block_totals(acc, a, b, c);
+    if (threadIdx.x == 0) {
+      const int sh = blockIdx.x % kCounterShards;
+      if (a) atomicAdd(&Rn->nf[sh], a);
+      if (b) atomicAdd(&Rn->mf[sh], b);
+      if (c) atomicAdd(&Rn->visdeg[sh], c);
+      s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                  RoundDecision{&p, L, dir});
     }
-    if (dir == kPull) ++pull_rounds;
-    visited += nf;
-    if (nf == 0) {
-      L += 1;
-      break;
-    }
-    if (L + 1 >= p.level_cap) {
-      if (leader) atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
-      L += 1;
-      ok = false;
-      break;
-    }
-    const int next = next_direction(p, dir, nf, prev_nf, mf, explored);
-    explored += vd;
+    __syncthreads();
+    const unsigned payload = s_payload;
+    if (payload == kWaitFailed || (payload & kDone)) break;
     queued = dir == kPush;  // a push round queued F_{L+1}; a pull round did not
-    if (next != dir) ++switches;
-    prev_nf = nf;
-    dir = next;
+    dir = (payload & kNextPull) ? kPull : kPush;
+    uint32_t *t = fr2;  // rotate: F_{L+1} becomes the frontier
+    fr2 = fr0;
+    fr0 = fr1;
+    fr1 = t;
     ++L;
   }
-  if (leader) {
-    cg_stats *st = p.stats;
-    if (L > 0 && L - 1 < CG_HISTORY) st->round_ns[L - 1] = global_ns() - t_round;
-    st->finish_ns = 0;
-    st->status = *(volatile int *)&ctl->status;
-    st->rounds = L;
-    st->visited = (int64_t)visited;
-    st->pull_rounds = pull_rounds;
-    st->switches = switches;
-    st->history_len = L < CG_HISTORY ? L : CG_HISTORY;
-    st->device_ms = 0.f;
-  }
+  if (leader && s_payload == kWaitFailed) p.stats->status = *(volatile int *)&ctl->status;
 }
 
 // Graph500 m per search (bfs_timing.py:379-398), lane = blockIdx.y.

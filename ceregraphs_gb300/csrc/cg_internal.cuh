@@ -26,8 +26,10 @@ namespace cg {
 
 // Grid-wide wait state: blocks arrive on one of kWaitGroups group counters
 // (blockIdx % kWaitGroups), the last of each group on the top counter, the
-// last group releases the generation word.  Each counter has its own
-// 128-byte line so arrivals of different groups do not serialise.
+// last group releases the sync word: generation in the low 32 bits and a
+// 32-bit payload (the decision the last arrival took for everyone) in the
+// high bits.  Each counter has its own 128-byte line so arrivals of
+// different groups do not serialise.
 constexpr int kWaitGroups = 16;
 struct GridWaitGroup {
   unsigned int count;
@@ -35,8 +37,9 @@ struct GridWaitGroup {
 };
 struct GridWait {
   unsigned int top;
-  unsigned int gen;
-  unsigned int pad[30];
+  unsigned int pad0;
+  unsigned long long sync;
+  unsigned int pad[28];
   GridWaitGroup group[kWaitGroups];
 };
 
@@ -62,14 +65,21 @@ struct RoundRec {
   unsigned long long pad[6];
 };
 
+// Only the block that arrives last at a round's grid-wide wait reads and
+// writes the round bookkeeping (prev_nf .. t_round); the waits order these
+// accesses from round to round.
 struct BfsCtl {
-  GridWait wait;               // own 128-byte line
+  GridWait wait;               // own 128-byte lines
   int status;
-  int rounds;
-  unsigned long long visited;
   int pull_rounds;
   int switches;
-  int pad[26];
+  int pad0;
+  unsigned long long visited;
+  unsigned long long prev_nf;
+  unsigned long long explored;
+  long long t_start;
+  long long t_round;
+  unsigned long long pad[9];
   RoundRec rec[kRing];
 };
 
@@ -161,17 +171,6 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-// Grid-wide wait for a cooperative launch (all blocks co-resident).  Thread 0
-// of each block arrives on its group counter with an acquire-release add
-// (releasing the block's writes, ordered before it by __syncthreads); the last
-// arrival of a group resets that counter and arrives on the top counter the
-// same way; the last group resets the top counter and releases the
-// generation word, which everyone else polls with acquire loads.  Every wait
-// is bounded: after `timeout_ns` (or once another block has flagged an error)
-// the block records CG_ERR_TIMEOUT and the caller leaves its loop, so a wait
-// that can never complete ends the kernel instead of spinning.  `extra` > 0
-// makes the top counter expect that many arrivals that never come (the test
-// hook behind cg_options.test_unmatched_wait).
 __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
   unsigned old;
   asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
@@ -179,41 +178,73 @@ __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
   return old;
 }
 
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+constexpr unsigned kWaitFailed = 0xffffffffu;
+
+// Grid-wide wait for a cooperative launch (all blocks co-resident), called by
+// thread 0 of each block after a __syncthreads.  The thread arrives on its
+// group counter with an acquire-release add (releasing the block's writes,
+// ordered before it by the __syncthreads); the last arrival of a group resets
+// that counter and arrives on the top counter the same way; the last group
+// resets the top counter, runs `decide()` (it sees every block's writes) and
+// releases the sync word with the next generation and decide()'s payload.
+// Everyone else polls the sync word with acquire loads and gets the payload.
+// Every wait is bounded: after `timeout_ns` (or once another block has
+// flagged an error) the thread records CG_ERR_TIMEOUT and returns
+// kWaitFailed, so a wait that can never complete ends the kernel instead of
+// spinning.  `extra` > 0 makes the top counter expect that many arrivals that
+// never come (the test hook behind cg_options.test_unmatched_wait).
+template <class Decide>
+__device__ __forceinline__ unsigned arrive_and_wait(GridWait *w, int *status,
+                                                    long long timeout_ns, unsigned extra,
+                                                    Decide decide) {
+  const unsigned long long s0 = ld_acquire64(&w->sync);
+  const unsigned g = (unsigned)s0;
+  const unsigned groups = gridDim.x < (unsigned)kWaitGroups ? gridDim.x : kWaitGroups;
+  const unsigned grp = blockIdx.x % kWaitGroups;
+  const unsigned members = (gridDim.x - grp + kWaitGroups - 1) / kWaitGroups;
+  if (atom_add_acq_rel(&w->group[grp].count, 1u) + 1u == members) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->group[grp].count) : "memory");
+    if (atom_add_acq_rel(&w->top, 1u) + 1u == groups + extra) {
+      asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->top) : "memory");
+      const unsigned payload = decide();
+      const unsigned long long word =
+          (unsigned long long)(g + 1u) | ((unsigned long long)payload << 32);
+      asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(&w->sync), "l"(word) : "memory");
+      return payload;
+    }
+  }
+  long long t0 = 0;
+  unsigned spins = 0;
+  while (true) {
+    const unsigned long long s1 = ld_acquire64(&w->sync);
+    if ((unsigned)s1 != g) return (unsigned)(s1 >> 32);
+    if ((++spins & 255u) == 0) {
+      if (t0 == 0) t0 = global_ns();
+      if (*(volatile int *)status != 0 || global_ns() - t0 > timeout_ns) {
+        atomicCAS(status, 0, (int)CG_ERR_TIMEOUT);
+        return kWaitFailed;
+      }
+    }
+  }
+}
+
+struct NoDecision {
+  __device__ unsigned operator()() const { return 0u; }
+};
+
+// Block-wide form without a decision: all threads call; false on timeout.
 __device__ __forceinline__ bool grid_wait(GridWait *w, int *status, long long timeout_ns,
                                           unsigned extra = 0) {
   __shared__ int s_ok;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned g = ld_acquire(&w->gen);
-    const unsigned groups = gridDim.x < (unsigned)kWaitGroups ? gridDim.x : kWaitGroups;
-    const unsigned grp = blockIdx.x % kWaitGroups;
-    const unsigned members = (gridDim.x - grp + kWaitGroups - 1) / kWaitGroups;
-    bool released = false;
-    if (atom_add_acq_rel(&w->group[grp].count, 1u) + 1u == members) {
-      asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->group[grp].count) : "memory");
-      if (atom_add_acq_rel(&w->top, 1u) + 1u == groups + extra) {
-        asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&w->top) : "memory");
-        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&w->gen) : "memory");
-        released = true;
-      }
-    }
-    if (!released) {
-      long long t0 = 0;
-      unsigned spins = 0;
-      while (ld_acquire(&w->gen) == g) {
-        if ((++spins & 255u) == 0) {
-          if (t0 == 0) t0 = global_ns();
-          if (*(volatile int *)status != 0 || global_ns() - t0 > timeout_ns) {
-            atomicCAS(status, 0, (int)CG_ERR_TIMEOUT);
-            ok = 0;
-            break;
-          }
-        }
-      }
-    }
-    s_ok = ok;
-  }
+  if (threadIdx.x == 0)
+    s_ok = arrive_and_wait(w, status, timeout_ns, extra, NoDecision()) != kWaitFailed;
   __syncthreads();
   return s_ok != 0;
 }

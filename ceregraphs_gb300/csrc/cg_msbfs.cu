@@ -20,7 +20,7 @@
 // walked by one warp: each round their in-list is cut into kHubChunk pieces
 // scanned by different warps, which combine per-lane parent candidates with
 // atomicMin in a small per-hub buffer; a finalize phase then writes the hub's
-// outputs and queues it (hubq[2], a separate frontier list).
+// outputs and queues it after the round's other discoveries.
 //
 // Pull round: every non-hub vertex with unvisited lanes whose search is still
 // running scans its ascending in-list and takes, per lane, the first frontier
@@ -30,6 +30,9 @@
 // candidates by atomicMin instead; a resolve phase scans each newly reached
 // non-hub vertex's ascending in-list for its parents.
 #include <cuda_runtime.h>
+#include <string.h>
+
+#include <new>
 
 #include "cg_internal.cuh"
 
@@ -46,17 +49,37 @@ struct MsRound {
   unsigned long long nf[kCounterShards];      // vertices with a nonzero frontier mask
   unsigned long long visits[kCounterShards];  // lane discoveries
   unsigned long long mf[kCounterShards];      // sum of out-degrees over the frontier
-  unsigned long long big;       // main queue: (count << 32) | edges of its big vertices
-  unsigned long long hub;       // hub queue:  (count << 32) | edges
+  unsigned long long big;       // queue: (count << 32) | edges of its big vertices
   unsigned int nlight, work;
+  unsigned int res_light, res_big;  // queue counts a push round's resolve phase covers
   unsigned long long lanes[2];  // lanes whose frontier is non-empty
   unsigned long long pad[2];
 };
 
+// Lane table of a serving pool: where each lane's outputs go and the round at
+// which its search started (its level = round + 1 - start).
+struct LaneTable {
+  int32_t *levels[kMsMaxLanes];
+  int32_t *parents[kMsMaxLanes];
+  int32_t start[kMsMaxLanes];
+};
+
+// Only the block that arrives last at a round's grid-wide wait touches the
+// round bookkeeping (L .. t_round); the waits order those accesses.  L and
+// dir persist between launches, so a serving pool resumes where it stopped.
 struct MsCtl {
   GridWait wait;
   int status;
-  int pad[31];
+  int L;                          // next round to run
+  int dir;                        // its direction (0 push, 1 pull)
+  int pull_rounds;
+  int switches;
+  int pad0;
+  unsigned long long visited;
+  unsigned long long done[2];     // lanes whose search ended (cleared by the host)
+  long long t_start;
+  long long t_round;
+  unsigned long long pad[8];
   MsRound rec[kRing];
 };
 
@@ -70,15 +93,14 @@ struct MsParams {
   uint32_t *touched0, *touched1;
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
-  int32_t *hubq0, *hubq1;
-  uint32_t *huboff0, *huboff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
   const int32_t *hub_vtx;    // [nhub]
   const uint32_t *hub_choff; // [nhub + 1] prefix of in-list chunks
   uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
   uint64_t *hub_found;       // [nhub][W] lanes found this round
   int nhub;
-  int32_t *levels, *parents;  // root-major, k x n
+  int32_t *levels, *parents;  // batch mode: lane l at levels + l * n (start round 0)
+  const LaneTable *lanes;     // serving pool: per-lane outputs and start rounds
   MsCtl *ctl;
   cg_stats *stats;
   int k;
@@ -86,6 +108,10 @@ struct MsParams {
   float ms_alpha;
   int level_cap;
   long long timeout_ns;
+  int resume;                 // continue from ctl->L instead of clearing and seeding
+  int max_rounds;             // stop after this many rounds in this launch
+  int stop_on_finish;         // stop after a round in which some lane's search ended
+  int finish_all;             // write -1 for every unreached (lane, vertex) at the end
   int32_t roots[kMsMaxLanes];
 };
 
@@ -180,19 +206,31 @@ __device__ __forceinline__ Mask<W> warp_or(Mask<W> m) {
   return m;
 }
 
+// Output of lane l for vertex v discovered in round `round` (level round + 1
+// for a batch; relative to the lane's start round in a serving pool).
+__device__ __forceinline__ void write_lane(const MsParams &p, int l, int64_t v, int32_t parent,
+                                           int round) {
+  if (p.lanes) {
+    p.lanes->levels[l][v] = round + 1 - p.lanes->start[l];
+    p.lanes->parents[l][v] = parent;
+  } else {
+    const int64_t at = (int64_t)l * p.n + v;
+    p.levels[at] = round + 1;
+    p.parents[at] = parent;
+  }
+}
+
 // Writes level and parent of vertex v for every lane in `m`.
 template <int W>
 __device__ __forceinline__ void write_lanes(const MsParams &p, int64_t v, const Mask<W> &m,
-                                            int32_t parent, int level) {
+                                            int32_t parent, int round) {
 #pragma unroll
   for (int i = 0; i < W; ++i) {
     uint64_t bits = m.w[i];
     while (bits) {
       const int b = __ffsll((long long)bits) - 1;
       bits &= bits - 1;
-      const int64_t at = (int64_t)(i * 64 + b) * p.n + v;
-      p.levels[at] = level;
-      p.parents[at] = parent;
+      write_lane(p, i * 64 + b, v, parent, round);
     }
   }
 }
@@ -259,71 +297,6 @@ __device__ __forceinline__ unsigned long long ms_warp_sum(unsigned long long x) 
   return x;
 }
 
-__device__ void ms_flush(MsAcc &acc, MsRound *Rn) {
-  __shared__ unsigned long long s_red[3][kMsBlock / 32];
-  __shared__ unsigned long long s_lanes[2];
-  const int lane = lane_id(), wib = threadIdx.x >> 5;
-  if (threadIdx.x < 2) s_lanes[threadIdx.x] = 0ull;
-  unsigned long long a = ms_warp_sum(acc.nf), b = ms_warp_sum(acc.visits),
-                     c = ms_warp_sum(acc.mf);
-  unsigned long long l0 = acc.lanes[0], l1 = acc.lanes[1];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    l0 |= __shfl_xor_sync(kMsFull, l0, o);
-    l1 |= __shfl_xor_sync(kMsFull, l1, o);
-  }
-  if (lane == 0) {
-    s_red[0][wib] = a;
-    s_red[1][wib] = b;
-    s_red[2][wib] = c;
-  }
-  __syncthreads();
-  if (lane == 0) {
-    if (l0) atomicOr(&s_lanes[0], l0);
-    if (l1) atomicOr(&s_lanes[1], l1);
-  }
-  __syncthreads();
-  if (wib == 0) {
-    const int nw = blockDim.x >> 5;
-    a = ms_warp_sum(lane < nw ? s_red[0][lane] : 0ull);
-    b = ms_warp_sum(lane < nw ? s_red[1][lane] : 0ull);
-    c = ms_warp_sum(lane < nw ? s_red[2][lane] : 0ull);
-    if (lane == 0) {
-      const int sh = blockIdx.x % kCounterShards;
-      if (a) atomicAdd(&Rn->nf[sh], a);
-      if (b) atomicAdd(&Rn->visits[sh], b);
-      if (c) atomicAdd(&Rn->mf[sh], c);
-      if (s_lanes[0]) atomicOr(&Rn->lanes[0], s_lanes[0]);
-      if (s_lanes[1]) atomicOr(&Rn->lanes[1], s_lanes[1]);
-    }
-  }
-  __syncthreads();
-  acc = MsAcc();
-}
-
-// Totals of the sharded round counters after a grid-wide wait (all threads of
-// the block call; every block gets the same values).
-__device__ void ms_read_counters(const MsRound *R, unsigned long long &nf,
-                                 unsigned long long &visits, unsigned long long &mf) {
-  __shared__ unsigned long long s_tot[3];
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    const int which = lane / kCounterShards, sh = lane % kCounterShards;
-    unsigned long long x = 0;
-    if (which == 0) x = *(volatile const unsigned long long *)&R->nf[sh];
-    else if (which == 1) x = *(volatile const unsigned long long *)&R->visits[sh];
-    else if (which == 2) x = *(volatile const unsigned long long *)&R->mf[sh];
-#pragma unroll
-    for (int o = kCounterShards / 2; o > 0; o >>= 1) x += __shfl_xor_sync(kMsFull, x, o);
-    if (sh == 0 && which < 3) s_tot[which] = x;
-  }
-  __syncthreads();
-  nf = s_tot[0];
-  visits = s_tot[1];
-  mf = s_tot[2];
-  __syncthreads();
-}
-
 // Warp-cooperative scan of in-list entries [s, e) of vertex v (all lanes call
 // with the same arguments): 32 sources per step; for each lane bit found in a
 // step, the lowest warp lane holding it -- the smallest source -- wins.  Stops
@@ -352,13 +325,10 @@ __device__ Mask<W> warp_scan(const MsParams &p, int64_t v, int64_t s, int64_t e,
           bits &= bits - 1;
           const unsigned who = __ballot_sync(kMsFull, (f.w[j] >> b) & 1ull);
           if (lane == __ffs(who) - 1) {
-            if (hub >= 0) {
+            if (hub >= 0)
               atomicMin(p.hub_cand + (int64_t)hub * (64 * W) + j * 64 + b, (unsigned)u);
-            } else {
-              const int64_t at = (int64_t)(j * 64 + b) * p.n + v;
-              p.levels[at] = level;
-              p.parents[at] = u;
-            }
+            else
+              write_lane(p, j * 64 + b, v, u, level);
           }
         }
       }
@@ -374,15 +344,28 @@ template <int W>
 __device__ __forceinline__ Mask<W> thread_scan(const MsParams &p, int64_t v, int64_t s, int64_t e,
                                                const Mask<W> &want, const uint64_t *cur,
                                                int level) {
+  // four sources at a time: their index and mask loads are all in flight
+  // together; the four are then taken in ascending order
+  constexpr int G = 4;
   Mask<W> got = Mask<W>::zero();
-  for (int64_t i = s; i < e; ++i) {
-    const int32_t u = __ldg(p.in_idx + i);
-    const Mask<W> f = (ld_mask<W>(cur, u) & want).andnot(got);
-    if (f.any()) {
-      write_lanes<W>(p, v, f, u, level);
-      got = got | f;
-      if (got == want) break;
+  for (int64_t i0 = s; i0 < e; i0 += G) {
+    int32_t u[G];
+    Mask<W> m[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) u[k] = i0 + k < e ? __ldg(p.in_idx + i0 + k) : -1;
+#pragma unroll
+    for (int k = 0; k < G; ++k) m[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+    bool done = false;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const Mask<W> f = (m[k] & want).andnot(got);
+      if (f.any()) {
+        write_lanes<W>(p, v, f, u[k], level);
+        got = got | f;
+        if (got == want) done = true;
+      }
     }
+    if (done) break;
   }
   return got;
 }
@@ -453,8 +436,8 @@ __device__ void hub_finalize(const MsParams &p, int L, uint64_t *nxt, MsRound *R
   const int lane = lane_id();
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int next_parity = (L + 1) & 1;
-  int32_t *hq = next_parity ? p.hubq1 : p.hubq0;
-  uint32_t *hoff = next_parity ? p.huboff1 : p.huboff0;
+  int32_t *q = next_parity ? p.queue1 : p.queue0;
+  uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
   for (int h = warp_id_global(); h < p.nhub; h += nwarps) {
     const Mask<W> found = ld_mask<W>(p.hub_found, h);
     if (!found.any()) continue;
@@ -466,9 +449,7 @@ __device__ void hub_finalize(const MsParams &p, int L, uint64_t *nxt, MsRound *R
         const int b = lane + 32 * half;
         if ((found.w[j] >> b) & 1ull) {
           uint32_t *cand = p.hub_cand + (int64_t)h * (64 * W) + j * 64 + b;
-          const int64_t at = (int64_t)(j * 64 + b) * p.n + v;
-          p.levels[at] = L + 1;
-          p.parents[at] = (int32_t)*cand;
+          write_lane(p, j * 64 + b, v, (int32_t)*cand, L);
           *cand = 0xffffffffu;
         }
       }
@@ -482,9 +463,9 @@ __device__ void hub_finalize(const MsParams &p, int L, uint64_t *nxt, MsRound *R
       acc_lanes<W>(acc, found);
       deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
     }
-    // every hub is "big" in the hub list (no light section is used)
-    ms_enqueue(lane == 0, v, deg > kLightMax ? deg : kLightMax + 1, hq, p.nhub, hoff,
-               &Rn->work /* unused: hubs are never light */, &Rn->hub, acc);
+    // queued after every other vertex of the next frontier (a push round's
+    // resolve phase only walks the queue as it stood before this phase)
+    ms_enqueue(lane == 0, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
 }
 
@@ -513,7 +494,7 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       }
     }
     if (!__ballot_sync(kMsFull, want.any())) continue;
-    const Mask<W> got = scan_group<W>(p, v, s, e, want, cur, L + 1);
+    const Mask<W> got = scan_group<W>(p, v, s, e, want, cur, L);
     bool claimed = false;
     int64_t deg = 0;
     if (got.any()) {
@@ -526,7 +507,7 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     }
     ms_enqueue(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
-  if (p.nhub > 0) hub_chunks<W>(p, cur, active, L + 1);
+  if (p.nhub > 0) hub_chunks<W>(p, cur, active, L);
 }
 
 // Edge u -> v of a push round.  Hub targets take parent candidates directly;
@@ -644,31 +625,22 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   const int parity = L & 1, next_parity = parity ^ 1;
   const int32_t *qc = parity ? p.queue1 : p.queue0;
   const uint32_t *bc = parity ? p.bigoff1 : p.bigoff0;
-  const int32_t *hc = parity ? p.hubq1 : p.hubq0;
-  const uint32_t *hbc = parity ? p.huboff1 : p.huboff0;
   int32_t *qn = next_parity ? p.queue1 : p.queue0;
   uint32_t *bn = next_parity ? p.bigoff1 : p.bigoff0;
 
   const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
-  const unsigned long long hubw = *(volatile unsigned long long *)&Rc->hub;
   const unsigned nbig = (unsigned)(bigw >> 32), big_edges = (unsigned)bigw;
-  const unsigned nhubf = (unsigned)(hubw >> 32), hub_edges = (unsigned)hubw;
   const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
   const unsigned nb = (big_edges + kPushChunk - 1) / kPushChunk;
-  const unsigned nh = (hub_edges + kPushChunk - 1) / kPushChunk;
-  const unsigned nitems = nb + nh + (nlight + 31u) / 32u;
+  const unsigned nitems = nb + (nlight + 31u) / 32u;
   unsigned item = (unsigned)warp_id_global();
   while (item < nitems) {
     if (item < nb) {
       const unsigned x0 = item * kPushChunk;
       ms_push_chunk<W>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0,
                        min(x0 + (unsigned)kPushChunk, big_edges), qn, bn, Rn, acc);
-    } else if (item < nb + nh) {
-      const unsigned x0 = (item - nb) * kPushChunk;
-      ms_push_chunk<W>(p, cur, nxt, touched, hc, p.nhub, hbc, nhubf, x0,
-                       min(x0 + (unsigned)kPushChunk, hub_edges), qn, bn, Rn, acc);
     } else {
-      const unsigned idx = (item - nb - nh) * 32u + lane;
+      const unsigned idx = (item - nb) * 32u + lane;
       int32_t u = -1;
       int64_t s = 0, d = 0;
       if (idx < nlight) {
@@ -726,8 +698,8 @@ __device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, uint64
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
   const int32_t *q = next_parity ? p.queue1 : p.queue0;
-  const int64_t nl = *(volatile unsigned *)&Rn->nlight;
-  const int64_t nbg = (int64_t)(*(volatile unsigned long long *)&Rn->big >> 32);
+  const int64_t nl = *(volatile unsigned *)&Rn->res_light;
+  const int64_t nbg = *(volatile unsigned *)&Rn->res_big;
   const int64_t total = nl + nbg;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total;
        base += nthreads) {
@@ -743,78 +715,224 @@ __device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, uint64
       s = __ldg(p.in_off + v);
       e = __ldg(p.in_off + v + 1);
     }
-    scan_group<W>(p, v, s, e, nw, cur, L + 1);
+    scan_group<W>(p, v, s, e, nw, cur, L);
   }
   if (p.nhub > 0) hub_finalize<W>(p, L, nxt, Rn, acc);
 }
 
+// Block totals of the per-thread counters (thread 0 gets them) -- the one
+// __syncthreads of a round's end before the grid-wide wait.
+__device__ void ms_block_totals(MsAcc &acc, MsAcc &tot) {
+  __shared__ unsigned long long s_red[5][kMsBlock / 32];
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+  const unsigned long long a = ms_warp_sum(acc.nf), b = ms_warp_sum(acc.visits),
+                           c = ms_warp_sum(acc.mf);
+  unsigned long long l0 = acc.lanes[0], l1 = acc.lanes[1];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l0 |= __shfl_xor_sync(kMsFull, l0, o);
+    l1 |= __shfl_xor_sync(kMsFull, l1, o);
+  }
+  if (lane == 0) {
+    s_red[0][wib] = a;
+    s_red[1][wib] = b;
+    s_red[2][wib] = c;
+    s_red[3][wib] = l0;
+    s_red[4][wib] = l1;
+  }
+  __syncthreads();
+  tot = MsAcc();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      tot.nf += s_red[0][i];
+      tot.visits += s_red[1][i];
+      tot.mf += s_red[2][i];
+      tot.lanes[0] |= s_red[3][i];
+      tot.lanes[1] |= s_red[4][i];
+    }
+  }
+  acc = MsAcc();
+}
+
+constexpr unsigned kMsStop = 1u, kMsNextPull = 2u;
+
+// End of round L, run by the block that arrives last: termination (no lane
+// has a frontier), lanes whose search ended this round, the direction of the
+// next round, statistics, and the reset of the record round L + 1 fills.
+template <int W>
+__device__ unsigned ms_decide(const MsParams &p, int L, int dir, int ran) {
+  MsCtl *ctl = p.ctl;
+  const MsRound *Rc = &ctl->rec[L % kRing];
+  const MsRound *Rn = &ctl->rec[(L + 1) % kRing];
+  unsigned long long nf = 0, visits = 0, mf = 0;
+#pragma unroll
+  for (int i = 0; i < kCounterShards; ++i) {
+    nf += *(volatile const unsigned long long *)&Rn->nf[i];
+    visits += *(volatile const unsigned long long *)&Rn->visits[i];
+    mf += *(volatile const unsigned long long *)&Rn->mf[i];
+  }
+  bool finished = false;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const unsigned long long ended = *(volatile const unsigned long long *)&Rc->lanes[i] &
+                                     ~*(volatile const unsigned long long *)&Rn->lanes[i];
+    if (ended) {
+      ctl->done[i] |= ended;
+      finished = true;
+    }
+  }
+  cg_stats *st = p.stats;
+  const long long now = global_ns();
+  if (ran < CG_HISTORY) {
+    st->nf_history[ran] = (int64_t)visits;
+    st->direction_history[ran] = dir;
+    st->round_ns[ran] = now - ctl->t_round;
+  }
+  ctl->t_round = now;
+  if (dir == 1) ctl->pull_rounds += 1;
+  ctl->visited += visits;
+  bool stop = nf == 0 || ran + 1 >= p.max_rounds || (p.stop_on_finish && finished);
+  if (nf != 0 && L + 1 >= p.level_cap) {
+    atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
+    stop = true;
+  }
+  int next;
+  if (p.direction == CG_DIR_TOPDOWN)
+    next = 0;
+  else if (p.direction == CG_DIR_BOTTOMUP)
+    next = 1;
+  else
+    next = ((double)mf * (double)p.ms_alpha > (double)p.nnz) ? 1 : 0;
+  if (next != dir) ctl->switches += 1;
+  ctl->L = L + 1;
+  ctl->dir = next;
+  MsRound *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
+  for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->visits[i] = Rz->mf[i] = 0;
+  Rz->big = 0;
+  Rz->res_light = Rz->res_big = 0;
+  Rz->nlight = Rz->work = 0;
+  Rz->lanes[0] = Rz->lanes[1] = 0;
+  if (stop) {
+    const int rounds = ran + 1;
+    st->status = *(volatile int *)&ctl->status;
+    st->rounds = rounds;
+    st->visited = (int64_t)ctl->visited;
+    st->pull_rounds = ctl->pull_rounds;
+    st->switches = ctl->switches;
+    st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
+    st->device_ms = 0.f;
+  }
+  return (stop ? kMsStop : 0u) | (next ? kMsNextPull : 0u);
+}
+
+template <int W>
+struct MsRoundDecision {
+  const MsParams *p;
+  int L, dir, ran;
+  __device__ unsigned operator()() const { return ms_decide<W>(*p, L, dir, ran); }
+};
+
+// At the wait between a push round's push and resolve phases: the queue as
+// it stands then (hubs finalized during resolve are appended after it).
+struct ResolveSnapshot {
+  MsRound *R;
+  __device__ unsigned operator()() const {
+    R->res_light = *(volatile unsigned *)&R->nlight;
+    R->res_big = (unsigned)(*(volatile unsigned long long *)&R->big >> 32);
+    return 0u;
+  }
+};
+
+struct MsSetupDecision {
+  MsCtl *ctl;
+  cg_stats *st;
+  __device__ unsigned operator()() const {
+    const long long now = global_ns();
+    st->setup_ns = now - ctl->t_start;
+    ctl->t_round = now;
+    ctl->pull_rounds = 0;
+    ctl->switches = 0;
+    return 0u;
+  }
+};
+
+// One launch runs rounds until every lane's search has ended, or max_rounds
+// rounds, or (stop_on_finish) a round in which some lane's search ended.
+// A fresh launch clears the lane state and seeds roots[0..k); a resumed one
+// (a serving pool) continues at round ctl->L with the lanes admitted since.
 template <int W>
 __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
+  __shared__ unsigned s_payload;
   MsCtl *ctl = p.ctl;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
-  const long long t_start = leader ? global_ns() : 0;
+  if (leader) ctl->t_start = global_ns();
   uint64_t *fr[3] = {p.fr0, p.fr1, p.fr2};
 
-  // phase 0: clear the lane state
-  for (int64_t i = gtid; i < p.n * W; i += nthreads) {
-    p.vis[i] = 0;
-    p.fr0[i] = 0;
-    p.fr1[i] = 0;
-    p.fr2[i] = 0;
-  }
-  for (int64_t w = gtid; w < p.words; w += nthreads) {
-    p.touched0[w] = 0;
-    p.touched1[w] = 0;
-  }
-  bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
-  // seed: lane i starts at roots[i] (block 0)
-  if (ok && blockIdx.x == 0 && threadIdx.x < p.k) {
-    const int i = threadIdx.x;
-    const int32_t r = p.roots[i];
-    const unsigned long long bit = 1ull << (i & 63);
-    atomicOr(reinterpret_cast<unsigned long long *>(p.vis + (int64_t)r * W + (i >> 6)), bit);
-    atomicOr(reinterpret_cast<unsigned long long *>(p.fr0 + (int64_t)r * W + (i >> 6)), bit);
-    p.levels[(int64_t)i * p.n + r] = 0;
-    p.parents[(int64_t)i * p.n + r] = r;
-    bool first = true;
-    for (int j = 0; j < i; ++j) first = first && (p.roots[j] != r);
-    if (first) {
-      const int64_t deg = p.out_off[r + 1] - p.out_off[r];
-      MsRound *R0 = &ctl->rec[0];
-      if (deg <= kLightMax) {
-        p.queue0[atomicAdd(&R0->nlight, 1u)] = r;
-      } else {
-        // roots are queued one by one: a 64-bit add keeps index and offset paired
-        const unsigned long long old =
-            atomicAdd(&R0->big, (1ull << 32) | (unsigned long long)deg);
-        p.queue0[p.n - 1 - (int64_t)(old >> 32)] = r;
-        p.bigoff0[old >> 32] = (unsigned)old;
+  bool ok = true;
+  if (!p.resume) {
+    // phase 0: clear the lane state
+    for (int64_t i = gtid; i < p.n * W; i += nthreads) {
+      p.vis[i] = 0;
+      p.fr0[i] = 0;
+      p.fr1[i] = 0;
+      p.fr2[i] = 0;
+    }
+    for (int64_t w = gtid; w < p.words; w += nthreads) {
+      p.touched0[w] = 0;
+      p.touched1[w] = 0;
+    }
+    ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
+    // seed: lane i starts at roots[i] (block 0)
+    if (ok && blockIdx.x == 0 && threadIdx.x < p.k) {
+      const int i = threadIdx.x;
+      const int32_t r = p.roots[i];
+      const unsigned long long bit = 1ull << (i & 63);
+      atomicOr(reinterpret_cast<unsigned long long *>(p.vis + (int64_t)r * W + (i >> 6)), bit);
+      atomicOr(reinterpret_cast<unsigned long long *>(p.fr0 + (int64_t)r * W + (i >> 6)), bit);
+      p.levels[(int64_t)i * p.n + r] = 0;
+      p.parents[(int64_t)i * p.n + r] = r;
+      bool first = true;
+      for (int j = 0; j < i; ++j) first = first && (p.roots[j] != r);
+      if (first) {
+        const int64_t deg = p.out_off[r + 1] - p.out_off[r];
+        MsRound *R0 = &ctl->rec[0];
+        if (deg <= kLightMax) {
+          p.queue0[atomicAdd(&R0->nlight, 1u)] = r;
+        } else {
+          // roots are queued one by one: a 64-bit add keeps index and offset paired
+          const unsigned long long old =
+              atomicAdd(&R0->big, (1ull << 32) | (unsigned long long)deg);
+          p.queue0[p.n - 1 - (int64_t)(old >> 32)] = r;
+          p.bigoff0[old >> 32] = (unsigned)old;
+        }
+        atomicAdd(&R0->nf[0], 1ull);
+        atomicAdd(&R0->mf[0], (unsigned long long)deg);
       }
-      atomicAdd(&R0->nf[0], 1ull);
-      atomicAdd(&R0->mf[0], (unsigned long long)deg);
-    }
-    if (i == 0) {
-      const Mask<W> a0 = lane_mask<W>(p.k);
-      ctl->rec[0].lanes[0] = a0.w[0];
-      ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
+      if (i == 0) {
+        const Mask<W> a0 = lane_mask<W>(p.k);
+        ctl->rec[0].lanes[0] = a0.w[0];
+        ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
+        ctl->visited = (unsigned long long)p.k;
+        ctl->L = 0;
+        ctl->dir = 0;
+      }
     }
   }
-  if (ok) ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
+  if (ok) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                  MsSetupDecision{ctl, p.stats});
+    __syncthreads();
+    ok = s_payload != kWaitFailed;
+  }
 
-  int dir = 0;  // 0 push, 1 pull
-  int L = 0, pull_rounds = 0, switches = 0;
-  unsigned long long visited = (unsigned long long)p.k;
-  MsAcc acc;
-  long long t_round = leader ? global_ns() : 0;
-  if (leader) p.stats->setup_ns = t_round - t_start;
+  int L = ctl->L, dir = ctl->dir;  // ordered by the wait above
+  int ran = 0;
+  MsAcc acc, tot;
   while (ok) {
-    if (leader && L > 0 && L - 1 < CG_HISTORY) {
-      const long long now = global_ns();
-      p.stats->round_ns[L - 1] = now - t_round;
-      t_round = now;
-    }
     const uint64_t *cur = fr[L % 3];
     uint64_t *nxt = fr[(L + 1) % 3];
     uint64_t *old = fr[(L + 2) % 3];
@@ -822,15 +940,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
     uint32_t *touched_next = (L & 1) ? p.touched0 : p.touched1;
     MsRound *Rc = &ctl->rec[L % kRing];
     MsRound *Rn = &ctl->rec[(L + 1) % kRing];
-    // F_{L-1}, last round's touched bits and the record of round L-1 are no
-    // longer read by anyone; the record is next appended to in round L + 2
-    if (leader) {
-      MsRound *Rz = &ctl->rec[(L + 3) % kRing];
-      for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->visits[i] = Rz->mf[i] = 0;
-      Rz->big = Rz->hub = 0;
-      Rz->nlight = Rz->work = 0;
-      Rz->lanes[0] = Rz->lanes[1] = 0;
-    }
+    // F_{L-1} and last round's touched bits are no longer read by anyone
     for (int64_t i = gtid; i < p.n * W; i += nthreads) old[i] = 0;
     for (int64_t w = gtid; w < p.words; w += nthreads) touched_next[w] = 0;
     if (dir == 1) {
@@ -844,47 +954,42 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
       }
     } else {
       ms_push<W>(p, L, cur, nxt, touched, Rc, Rn, acc);
-      if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
+      __syncthreads();
+      if (threadIdx.x == 0)
+        s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                    ResolveSnapshot{Rn});
+      __syncthreads();
+      if (s_payload == kWaitFailed) {
+        ok = false;
+        break;
+      }
       ms_resolve<W>(p, L, cur, nxt, Rn, acc);
     }
-    ms_flush(acc, Rn);
-    if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
-    unsigned long long nf, visits, mf;
-    ms_read_counters(Rn, nf, visits, mf);
-    if (leader && L < CG_HISTORY) {
-      p.stats->nf_history[L] = (int64_t)visits;
-      p.stats->direction_history[L] = dir;
+    ms_block_totals(acc, tot);
+    if (threadIdx.x == 0) {
+      const int sh = blockIdx.x % kCounterShards;
+      if (tot.nf) atomicAdd(&Rn->nf[sh], tot.nf);
+      if (tot.visits) atomicAdd(&Rn->visits[sh], tot.visits);
+      if (tot.mf) atomicAdd(&Rn->mf[sh], tot.mf);
+      if (tot.lanes[0]) atomicOr(&Rn->lanes[0], tot.lanes[0]);
+      if (tot.lanes[1]) atomicOr(&Rn->lanes[1], tot.lanes[1]);
+      s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                  MsRoundDecision<W>{&p, L, dir, ran});
     }
-    if (dir == 1) ++pull_rounds;
-    visited += visits;
-    if (nf == 0) {
-      L += 1;
-      break;
-    }
-    if (L + 1 >= p.level_cap) {
-      if (leader) atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
-      L += 1;
+    __syncthreads();
+    const unsigned payload = s_payload;
+    if (payload == kWaitFailed) {
       ok = false;
       break;
     }
-    int next;
-    if (p.direction == CG_DIR_TOPDOWN)
-      next = 0;
-    else if (p.direction == CG_DIR_BOTTOMUP)
-      next = 1;
-    else
-      next = ((double)mf * (double)p.ms_alpha > (double)p.nnz) ? 1 : 0;
-    if (next != dir) ++switches;
-    dir = next;
+    if (payload & kMsStop) break;
+    dir = (payload & kMsNextPull) ? 1 : 0;
     ++L;
+    ++ran;
   }
-  long long t_finish = 0;
-  if (leader) {
-    t_finish = global_ns();
-    if (L > 0 && L - 1 < CG_HISTORY) p.stats->round_ns[L - 1] = t_finish - t_round;
-  }
-  // unreached lanes: level and parent -1 (each (lane, vertex) is written once)
-  if (ok) {
+  // batch: unreached lanes get level and parent -1 (each (lane, vertex) is
+  // written once); a serving pool does this per lane when the lane is done
+  if (ok && p.finish_all) {
     for (int64_t v = gtid; v < p.n; v += nthreads) {
       const Mask<W> m = ld_mask<W>(p.vis, v);
       for (int l = 0; l < p.k; ++l) {
@@ -895,17 +1000,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
       }
     }
   }
-  if (leader) {
-    cg_stats *st = p.stats;
-    st->finish_ns = global_ns() - t_finish;
-    st->status = *(volatile int *)&ctl->status;
-    st->rounds = L;
-    st->visited = (int64_t)visited;
-    st->pull_rounds = pull_rounds;
-    st->switches = switches;
-    st->history_len = L < CG_HISTORY ? L : CG_HISTORY;
-    st->device_ms = 0.f;
-  }
+  if (leader && !ok) p.stats->status = *(volatile int *)&ctl->status;
 }
 
 // ---------------------------------------------------------------------------
@@ -937,8 +1032,6 @@ struct MsState {
   uint32_t *touched = nullptr;
   int32_t *queue = nullptr;
   uint32_t *bigoff = nullptr;
-  int32_t *hubq = nullptr;
-  uint32_t *huboff = nullptr;
   int32_t *hub_slot = nullptr;
   int32_t *hub_vtx = nullptr;
   uint32_t *hub_choff = nullptr;
@@ -956,8 +1049,6 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->touched);
   cudaFree(s->queue);
   cudaFree(s->bigoff);
-  cudaFree(s->hubq);
-  cudaFree(s->huboff);
   cudaFree(s->hub_slot);
   cudaFree(s->hub_vtx);
   cudaFree(s->hub_choff);
@@ -1004,9 +1095,7 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
     const size_t nh = nhub > 0 ? nhub : 1;
     if (cudaMalloc(&s->hub_choff, sizeof(uint32_t) * (nh + 1)) != cudaSuccess ||
         cudaMalloc(&s->hub_cand, sizeof(uint32_t) * nh * 64 * s->lane_words) != cudaSuccess ||
-        cudaMalloc(&s->hub_found, sizeof(uint64_t) * nh * s->lane_words) != cudaSuccess ||
-        cudaMalloc(&s->hubq, sizeof(int32_t) * 2 * nh) != cudaSuccess ||
-        cudaMalloc(&s->huboff, sizeof(uint32_t) * 2 * nh) != cudaSuccess) {
+        cudaMalloc(&s->hub_found, sizeof(uint64_t) * nh * s->lane_words) != cudaSuccess) {
       rc = CG_ERR_OUT_OF_MEMORY;
       break;
     }
@@ -1039,10 +1128,8 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
   return rc;
 }
 
-static int ms_alloc_state(cg_graph *g, int lane_words) {
-  if (g->ms_ctl && g->ms_lane_words == lane_words) return CG_OK;
-  ms_free_state(reinterpret_cast<MsState *>(g->ms_ctl));
-  g->ms_ctl = nullptr;
+// Lane state for one batched search stream (a graph's batch state or a pool).
+static int ms_create_state(cg_graph *g, int lane_words, MsState **out) {
   MsState *s = new MsState();
   s->lane_words = lane_words;
   s->bcap = bfs_big_capacity(g->n, g->nnz);
@@ -1061,10 +1148,21 @@ static int ms_alloc_state(cg_graph *g, int lane_words) {
     ms_free_state(s);
     return rc;
   }
-  g->ms_ctl = s;
-  g->ms_lane_words = lane_words;
   g->device_bytes += bits + sizeof(uint32_t) * 2 * words + sizeof(int32_t) * 2 * g->n +
                      sizeof(uint32_t) * 2 * s->bcap + sizeof(MsCtl);
+  *out = s;
+  return CG_OK;
+}
+
+static int ms_alloc_state(cg_graph *g, int lane_words) {
+  if (g->ms_ctl && g->ms_lane_words == lane_words) return CG_OK;
+  ms_free_state(reinterpret_cast<MsState *>(g->ms_ctl));
+  g->ms_ctl = nullptr;
+  MsState *s = nullptr;
+  int rc = ms_create_state(g, lane_words, &s);
+  if (rc) return rc;
+  g->ms_ctl = s;
+  g->ms_lane_words = lane_words;
   return CG_OK;
 }
 
@@ -1088,17 +1186,9 @@ int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems) {
   return CG_OK;
 }
 
+// Fields of a launch shared by batches and serving pools.
 template <int W>
-static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
-                          int32_t *d_levels, int32_t *d_parents) {
-  int block = g->opt.block_size > 0 ? g->opt.block_size : kMsBlock;
-  if (block > kMsBlock) block = kMsBlock;
-  block = (block / 32) * 32;
-  if (block < 128) block = 128;  // seeding uses threads 0..k-1 of block 0
-  int per_sm = 0;
-  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msbfs_persistent<W>, block, 0));
-  if (per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
-  if (g->opt.blocks_per_sm > 0 && g->opt.blocks_per_sm < per_sm) per_sm = g->opt.blocks_per_sm;
+static MsParams ms_params(const cg_graph *g, const MsState *s) {
   MsParams p;
   p.n = g->n;
   p.nnz = g->nnz;
@@ -1119,36 +1209,45 @@ static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
   p.bigoff0 = s->bigoff;
   p.bigoff1 = s->bigoff + s->bcap;
   const int64_t nh = s->nhub > 0 ? s->nhub : 1;
-  p.hubq0 = s->hubq;
-  p.hubq1 = s->hubq + nh;
-  p.huboff0 = s->huboff;
-  p.huboff1 = s->huboff + nh;
   p.hub_slot = s->hub_slot;
   p.hub_vtx = s->hub_vtx;
   p.hub_choff = s->hub_choff;
   p.hub_cand = s->hub_cand;
   p.hub_found = s->hub_found;
   p.nhub = s->nhub;
-  p.levels = d_levels;
-  p.parents = d_parents;
+  p.levels = p.parents = nullptr;
+  p.lanes = nullptr;
   p.ctl = s->ctl;
   p.stats = g->d_stats;
-  p.k = k;
+  p.k = 0;
+  p.resume = 0;
+  p.max_rounds = 0x7fffffff;
+  p.stop_on_finish = 0;
+  p.finish_all = 0;
   p.direction = g->opt.direction == CG_DIR_TAU ? CG_DIR_AUTO : g->opt.direction;
   p.ms_alpha = g->opt.ms_alpha > 0 ? g->opt.ms_alpha : 4.f;
   p.level_cap = g->opt.level_cap > 0 ? g->opt.level_cap
                                      : (int)((g->n + 1) < 0x7fffffff ? g->n + 1 : 0x7fffffff);
   p.timeout_ns = (long long)(g->opt.wait_timeout_ms > 0 ? g->opt.wait_timeout_ms : 1000) * 1000000ll;
-  for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = i < k ? (int32_t)roots[i] : 0;
-  CG_CUDA(cudaMemsetAsync(s->ctl, 0, sizeof(MsCtl), g->stream));
-  // candidates start at "none"; a pass cut short by an error leaves them dirty
-  CG_CUDA(cudaMemsetAsync(s->hub_cand, 0xff, sizeof(uint32_t) * (size_t)nh * 64 * W, g->stream));
-  CG_CUDA(cudaMemsetAsync(s->hub_found, 0, sizeof(uint64_t) * (size_t)nh * W, g->stream));
+  for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = 0;
+  return p;
+}
+
+template <int W>
+static int ms_launch(const cg_graph *g, const MsParams &p, cudaStream_t stream) {
+  int block = g->opt.block_size > 0 ? g->opt.block_size : kMsBlock;
+  if (block > kMsBlock) block = kMsBlock;
+  block = (block / 32) * 32;
+  if (block < 128) block = 128;  // seeding uses threads 0..k-1 of block 0
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msbfs_persistent<W>, block, 0));
+  if (per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+  if (g->opt.blocks_per_sm > 0 && g->opt.blocks_per_sm < per_sm) per_sm = g->opt.blocks_per_sm;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(per_sm * g->num_sms);
   cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = 0;
-  cfg.stream = g->stream;
+  cfg.stream = stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
@@ -1156,6 +1255,30 @@ static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
   cfg.numAttrs = 1;
   CG_CUDA(cudaLaunchKernelEx(&cfg, msbfs_persistent<W>, p));
   return CG_OK;
+}
+
+// Clean control block and hub candidates for a fresh launch on `s`.
+template <int W>
+static int ms_reset(const MsState *s, cudaStream_t stream) {
+  const int64_t nh = s->nhub > 0 ? s->nhub : 1;
+  CG_CUDA(cudaMemsetAsync(s->ctl, 0, sizeof(MsCtl), stream));
+  CG_CUDA(cudaMemsetAsync(s->hub_cand, 0xff, sizeof(uint32_t) * (size_t)nh * 64 * W, stream));
+  CG_CUDA(cudaMemsetAsync(s->hub_found, 0, sizeof(uint64_t) * (size_t)nh * W, stream));
+  return CG_OK;
+}
+
+template <int W>
+static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
+                          int32_t *d_levels, int32_t *d_parents) {
+  MsParams p = ms_params<W>(g, s);
+  p.levels = d_levels;
+  p.parents = d_parents;
+  p.k = k;
+  p.finish_all = 1;
+  for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = i < k ? (int32_t)roots[i] : 0;
+  int rc = ms_reset<W>(s, g->stream);
+  if (rc) return rc;
+  return ms_launch<W>(g, p, g->stream);
 }
 
 int msbfs_launch(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels,
@@ -1176,4 +1299,245 @@ int msbfs_launch(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels
   return CG_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Serving pools: continuous batching over the lanes of one resumable launch.
+struct Admission {
+  int count;
+  int32_t lane[kMsMaxLanes];
+  int32_t root[kMsMaxLanes];
+};
+
+// Seeds admitted lanes into the frontier of the next round (ctl->L): visited
+// and frontier bit, level 0 / parent root, the root queued once for a push
+// round, the lane marked active.  One thread, in order, so roots shared by
+// several admissions are queued once.
+template <int W>
+__global__ void pool_admit_kernel(MsParams p, Admission a) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  MsCtl *ctl = p.ctl;
+  const int L = ctl->L;
+  uint64_t *fr[3] = {p.fr0, p.fr1, p.fr2};
+  uint64_t *cur = fr[L % 3];
+  MsRound *Rc = &ctl->rec[L % kRing];
+  int32_t *q = (L & 1) ? p.queue1 : p.queue0;
+  uint32_t *boff = (L & 1) ? p.bigoff1 : p.bigoff0;
+  for (int i = 0; i < a.count; ++i) {
+    const int l = a.lane[i];
+    const int32_t r = a.root[i];
+    const Mask<W> before = ld_mask<W>(cur, r);
+    p.vis[(int64_t)r * W + (l >> 6)] |= 1ull << (l & 63);
+    cur[(int64_t)r * W + (l >> 6)] |= 1ull << (l & 63);
+    p.lanes->levels[l][r] = 0;
+    p.lanes->parents[l][r] = r;
+    Rc->lanes[l >> 6] |= 1ull << (l & 63);
+    if (!before.any()) {
+      const int64_t deg = p.out_off[r + 1] - p.out_off[r];
+      if (deg <= kLightMax) {
+        q[Rc->nlight++] = r;
+      } else {
+        const unsigned long long old = Rc->big;
+        Rc->big = old + ((1ull << 32) | (unsigned long long)deg);
+        q[p.n - 1 - (int64_t)(old >> 32)] = r;
+        boff[old >> 32] = (unsigned)old;
+      }
+    }
+  }
+}
+
+// Lanes whose search ended (ctl->done): level and parent -1 for the vertices
+// they never reached, and their bits cleared from the visited masks so the
+// lanes can be admitted again.  The mask is copied to done_out.
+template <int W>
+__global__ void pool_finish_kernel(MsParams p, unsigned long long *done_out) {
+  const MsCtl *ctl = p.ctl;
+  Mask<W> done;
+#pragma unroll
+  for (int i = 0; i < W; ++i) done.w[i] = ctl->done[i];
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gtid == 0) {
+    done_out[0] = ctl->done[0];
+    done_out[1] = ctl->done[1];
+    done_out[2] = (unsigned long long)(unsigned)ctl->L;
+    done_out[3] = (unsigned long long)(unsigned)ctl->status;
+  }
+  if (!done.any()) return;
+  for (int64_t v = gtid; v < p.n; v += (int64_t)gridDim.x * blockDim.x) {
+    const Mask<W> m = ld_mask<W>(p.vis, v);
+    const Mask<W> missed = done.andnot(m);
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      uint64_t bits = missed.w[i];
+      while (bits) {
+        const int b = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        p.lanes->levels[i * 64 + b][v] = -1;
+        p.lanes->parents[i * 64 + b][v] = -1;
+      }
+    }
+    if ((m & done).any()) st_mask<W>(p.vis, v, m.andnot(done));
+  }
+}
+
 }  // namespace cg
+
+struct cg_pool {
+  cg_graph *g = nullptr;
+  int W = 1;
+  cg::MsState *s = nullptr;
+  cg::LaneTable *d_lanes = nullptr;
+  cg::LaneTable h_lanes{};
+  unsigned long long busy[2] = {0ull, 0ull};
+  cg::Admission pending{};
+  unsigned long long *d_out = nullptr;  // done[2], L, status
+  unsigned long long *h_out = nullptr;  // page-locked copy
+  int next_round = 0;
+};
+
+namespace cg {
+
+template <int W>
+static int pool_start(cg_pool *pl) {
+  MsParams p = ms_params<W>(pl->g, pl->s);
+  p.lanes = pl->d_lanes;
+  p.level_cap = 0x7fffffff;
+  p.max_rounds = 1;
+  int rc = ms_reset<W>(pl->s, pl->g->stream);
+  if (rc) return rc;
+  return ms_launch<W>(pl->g, p, pl->g->stream);  // k = 0: clears the lane state
+}
+
+template <int W>
+static int pool_step(cg_pool *pl, int max_rounds, int stop_on_finish) {
+  cg_graph *g = pl->g;
+  MsParams p = ms_params<W>(g, pl->s);
+  p.lanes = pl->d_lanes;
+  p.level_cap = 0x7fffffff;
+  p.resume = 1;
+  p.k = 64 * W;
+  p.max_rounds = max_rounds > 0 ? max_rounds : 0x7fffffff;
+  p.stop_on_finish = stop_on_finish;
+  if (pl->pending.count) {
+    CG_CUDA(cudaMemcpyAsync(pl->d_lanes, &pl->h_lanes, sizeof(LaneTable), cudaMemcpyHostToDevice,
+                            g->stream));
+    pool_admit_kernel<W><<<1, 32, 0, g->stream>>>(p, pl->pending);
+    CG_CUDA(cudaGetLastError());
+    pl->pending.count = 0;
+  }
+  int rc = ms_launch<W>(g, p, g->stream);
+  if (rc) return rc;
+  int blocks = (int)((g->n + 255) / 256);
+  if (blocks > g->num_sms * 8) blocks = g->num_sms * 8;
+  if (blocks < 1) blocks = 1;
+  pool_finish_kernel<W><<<blocks, 256, 0, g->stream>>>(p, pl->d_out);
+  CG_CUDA(cudaGetLastError());
+  CG_CUDA(cudaMemsetAsync(&pl->s->ctl->done, 0, sizeof(unsigned long long) * 2, g->stream));
+  CG_CUDA(cudaMemcpyAsync(pl->h_out, pl->d_out, sizeof(unsigned long long) * 4,
+                          cudaMemcpyDeviceToHost, g->stream));
+  CG_CUDA(cudaStreamSynchronize(g->stream));
+  return CG_OK;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" {
+
+int cg_pool_create(cg_graph *g, int32_t lane_words, cg_pool **out) {
+  if (!g || !out || (lane_words != 1 && lane_words != 2)) return CG_ERR_INVALID_ARG;
+  *out = nullptr;
+  cg_pool *pl = new (std::nothrow) cg_pool();
+  if (!pl) return CG_ERR_OUT_OF_MEMORY;
+  pl->g = g;
+  pl->W = lane_words;
+  int rc = ms_create_state(g, lane_words, &pl->s);
+  if (!rc && (cudaMalloc(&pl->d_lanes, sizeof(LaneTable)) != cudaSuccess ||
+              cudaMalloc(&pl->d_out, sizeof(unsigned long long) * 4) != cudaSuccess ||
+              cudaHostAlloc(&pl->h_out, sizeof(unsigned long long) * 4, cudaHostAllocDefault) !=
+                  cudaSuccess))
+    rc = CG_ERR_OUT_OF_MEMORY;
+  if (!rc) {
+    memset(&pl->h_lanes, 0, sizeof(LaneTable));
+    cudaMemsetAsync(pl->d_lanes, 0, sizeof(LaneTable), g->stream);
+    rc = lane_words == 2 ? pool_start<2>(pl) : pool_start<1>(pl);
+    if (!rc) {
+      cudaError_t e = cudaStreamSynchronize(g->stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "cg_pool_create");
+    }
+  }
+  int L0 = 0;
+  if (!rc && cudaMemcpy(&L0, &pl->s->ctl->L, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = CG_ERR_CUDA;
+  if (rc) {
+    cg_pool_destroy(pl);
+    return rc;
+  }
+  pl->next_round = L0;
+  *out = pl;
+  return CG_OK;
+}
+
+int cg_pool_destroy(cg_pool *pl) {
+  if (!pl) return CG_ERR_INVALID_ARG;
+  if (pl->g && pl->g->stream) cudaStreamSynchronize(pl->g->stream);
+  ms_free_state(pl->s);
+  cudaFree(pl->d_lanes);
+  cudaFree(pl->d_out);
+  if (pl->h_out) cudaFreeHost(pl->h_out);
+  delete pl;
+  return CG_OK;
+}
+
+int cg_pool_admit(cg_pool *pl, int64_t root, int32_t *d_levels, int32_t *d_parents,
+                  int32_t *lane_out) {
+  if (!pl || !d_levels || !d_parents || root < 0 || root >= pl->g->n) return CG_ERR_INVALID_ARG;
+  const int lanes = 64 * pl->W;
+  int l = -1;
+  for (int i = 0; i < lanes; ++i)
+    if (!((pl->busy[i >> 6] >> (i & 63)) & 1ull)) {
+      l = i;
+      break;
+    }
+  if (l < 0) return CG_ERR_ADMISSION;
+  pl->busy[l >> 6] |= 1ull << (l & 63);
+  pl->h_lanes.levels[l] = d_levels;
+  pl->h_lanes.parents[l] = d_parents;
+  pl->h_lanes.start[l] = pl->next_round;
+  Admission &a = pl->pending;
+  a.lane[a.count] = l;
+  a.root[a.count] = (int32_t)root;
+  a.count += 1;
+  if (lane_out) *lane_out = l;
+  return CG_OK;
+}
+
+int cg_pool_step(cg_pool *pl, int32_t max_rounds, int32_t stop_on_finish, uint64_t *done_out,
+                 int32_t *next_round) {
+  if (!pl) return CG_ERR_INVALID_ARG;
+  int rc = pl->W == 2 ? pool_step<2>(pl, max_rounds, stop_on_finish)
+                      : pool_step<1>(pl, max_rounds, stop_on_finish);
+  if (rc) return rc;
+  pl->next_round = (int)pl->h_out[2];
+  if (done_out) {
+    done_out[0] = pl->h_out[0];
+    done_out[1] = pl->h_out[1];
+  }
+  if (next_round) *next_round = pl->next_round;
+  return (int)pl->h_out[3];
+}
+
+int cg_pool_release(cg_pool *pl, int32_t lane) {
+  if (!pl || lane < 0 || lane >= 64 * pl->W) return CG_ERR_INVALID_ARG;
+  pl->busy[lane >> 6] &= ~(1ull << (lane & 63));
+  return CG_OK;
+}
+
+int cg_pool_info(const cg_pool *pl, int32_t *lanes, int32_t *busy) {
+  if (!pl) return CG_ERR_INVALID_ARG;
+  if (lanes) *lanes = 64 * pl->W;
+  if (busy) *busy = __builtin_popcountll(pl->busy[0]) + __builtin_popcountll(pl->busy[1]);
+  return CG_OK;
+}
+
+}  // extern "C"

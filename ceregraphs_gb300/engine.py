@@ -125,6 +125,12 @@ class Graph:
           "cg_graph_export")
     return GraphArrays(self.n, self.nnz, io, ii, oo, oi, self.symmetric)
 
+  def export_offsets(self):
+    """The resident CSR offsets (n + 1 int64) on the host."""
+    io = np.empty(self.n + 1, dtype=np.int64)
+    check(_lib.load().cg_graph_export(self._h, _ptr(io), None, None, None), "cg_graph_export")
+    return io
+
   # -- lifecycle -----------------------------------------------------------
   def close(self):
     if self._h is not None and self._h.value:

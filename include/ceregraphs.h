@@ -169,6 +169,28 @@ int cg_capture_end(cg_graph *g, cg_exec **out);
 int cg_exec_launch(cg_exec *e);
 int cg_exec_destroy(cg_exec *e);
 
+/* ---- serving: continuous batching ----------------------------------------
+ * A pool keeps up to 64 * lane_words searches in flight on one resident graph,
+ * as bit lanes of one resumable batched launch.  cg_pool_admit puts a query
+ * (root + device outputs of n int32 each) into a free lane; cg_pool_step runs
+ * up to max_rounds rounds for every lane in flight (stop_on_finish: stop after
+ * a round in which some lane's search ended), finishes the lanes that ended
+ * (their outputs are then complete) and returns them in done (2 words of lane
+ * bits) -- queries admitted between steps join the lanes already running.
+ * cg_pool_release frees a finished lane.  Every lane's result equals the
+ * single-root search (cg_bfs) of its root.  No reference counterpart: this is
+ * the query loop around the kernel that run_graph500.py:321-440 runs one root
+ * at a time.  CG_ERR_ADMISSION: no free lane. */
+typedef struct cg_pool cg_pool;
+int cg_pool_create(cg_graph *g, int32_t lane_words, cg_pool **out);
+int cg_pool_destroy(cg_pool *pool);
+int cg_pool_admit(cg_pool *pool, int64_t root, int32_t *d_levels, int32_t *d_parents,
+                  int32_t *lane);
+int cg_pool_step(cg_pool *pool, int32_t max_rounds, int32_t stop_on_finish, uint64_t *done,
+                 int32_t *next_round);
+int cg_pool_release(cg_pool *pool, int32_t lane);
+int cg_pool_info(const cg_pool *pool, int32_t *lanes, int32_t *busy);
+
 /* ---- construction on the device -------------------------------------------
  * Synthetic inputs and the edge-list -> CSR/CSC build run on the GPU.
  *

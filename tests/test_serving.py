@@ -1,0 +1,151 @@
+"""Serving: continuous batching of queries into the lanes of a resumable
+batched search.  Every query's result in the mix must equal the same query
+run alone (integer results: bit-exact)."""
+import numpy as np
+import pytest
+
+from ceregraphs_gb300 import generators, graph500, serving
+
+
+def test_poisson_arrivals_are_deterministic_and_sorted():
+  roots = {"a": [1, 2, 3], "b": [7, 8]}
+  x = serving.poisson_arrivals(1000.0, 200, roots, seed=6)
+  y = serving.poisson_arrivals(1000.0, 200, roots, seed=6)
+  assert x == y
+  ts = [t for t, _, _ in x]
+  assert ts == sorted(ts) and ts[0] > 0
+  assert {g for _, g, _ in x} == {"a", "b"}
+  assert all(r in roots[g] for _, g, r in x)
+  # mean inter-arrival close to 1 / rate
+  assert abs(np.mean(np.diff(ts)) - 1e-3) < 3e-4
+
+
+def test_report_summary():
+  rep = serving.ServeReport()
+  for i, lat in enumerate([1.0, 2.0, 3.0, 4.0]):
+    q = serving.Query(i, "g", 0, 0.0)
+    q.t_done = lat / 1e3
+    rep.queries.append(q)
+  rep.wall_s = 0.5
+  s = rep.summary()
+  assert s["queries"] == 4 and s["throughput_qps"] == 8.0
+  assert s["p50_ms"] == pytest.approx(2.5)
+
+
+def _alone(oracle_mod, a, root):
+  out_off, out_idx = a.out_lists()
+  lv, pa, _ = oracle_mod.bfs(out_off, out_idx, a.in_off, a.in_idx, root)
+  return lv, pa
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lane_words", [1, 2])
+def test_pool_lanes_join_mid_flight(built_lib, oracle_mod, lane_words):
+  import torch
+  from ceregraphs_gb300.engine import Graph
+  a = generators.rmat(14, 16, 1)
+  roots = graph500.pick_sources(a, 3 * 64 * lane_words, 4)
+  want = {r: _alone(oracle_mod, a, r) for r in set(roots)}
+  with Graph(a) as g:
+    pool = serving.Pool(g, lane_words)
+    bufs = {}
+    todo = list(roots)
+    inflight = {}
+    finished = 0
+    steps = 0
+    while todo or inflight:
+      # admit a few each step: later queries join searches already running
+      for _ in range(5):
+        if not todo:
+          break
+        lv = torch.empty(a.n, dtype=torch.int32, device="cuda")
+        pa = torch.empty(a.n, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        lane = pool.admit(todo[0], lv, pa)
+        if lane is None:
+          break
+        inflight[lane] = (todo.pop(0), lv, pa)
+      for lane in pool.step(max_rounds=1, stop_on_finish=False):
+        r, lv, pa = inflight.pop(lane)
+        wl, wp = want[r]
+        assert np.array_equal(lv.cpu().numpy(), wl), (r, lane)
+        assert np.array_equal(pa.cpu().numpy(), wp), (r, lane)
+        pool.release(lane)
+        finished += 1
+      steps += 1
+      assert steps < 10000
+    assert finished == len(roots)
+    pool.close()
+
+
+@pytest.mark.gpu
+def test_pool_directed_and_deep(built_lib, oracle_mod):
+  import torch
+  from ceregraphs_gb300.engine import Graph
+  for a, roots in ((generators.er_directed(12, 6, 9), [0, 3, 4000, 77, 1024]),
+                   (generators.grid2d(40), [0, 39, 820, 1599])):
+    with Graph(a) as g:
+      pool = serving.Pool(g, 1)
+      outs = {}
+
+      def collect(done):
+        for lane in done:
+          r, lv, pa = outs.pop(lane)
+          wl, wp = _alone(oracle_mod, a, r)
+          assert np.array_equal(lv.cpu().numpy(), wl) and np.array_equal(pa.cpu().numpy(), wp)
+          pool.release(lane)
+
+      for r in roots:
+        lv = torch.empty(a.n, dtype=torch.int32, device="cuda")
+        pa = torch.empty(a.n, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        outs[pool.admit(r, lv, pa)] = (r, lv, pa)
+        collect(pool.step(max_rounds=3, stop_on_finish=False))   # staggered starts
+      for _ in range(100000):
+        if not outs:
+          break
+        collect(pool.step(max_rounds=0, stop_on_finish=True))
+      assert not outs
+      pool.close()
+
+
+@pytest.mark.gpu
+def test_server_mix_equals_alone_under_hbm_budget(built_lib):
+  import torch
+  from ceregraphs_gb300.engine import Graph
+  arrays = {"rmat13": generators.rmat(13, 16, 2), "rmat15": generators.rmat(15, 8, 3)}
+  graphs = {k: Graph(a) for k, a in arrays.items()}
+  roots = {k: graph500.pick_sources(a, 500, 5) for k, a in arrays.items()}
+  arrivals = serving.poisson_arrivals(20000.0, 300, roots, seed=6)
+  alone = {}
+  for k, g in graphs.items():
+    for r in {r for _, gg, r in arrivals if gg == k}:
+      lv, pa, _ = g.bfs(r)
+      alone[(k, r)] = (lv, pa)
+  checked = []
+  peak = [0]
+
+  def on_done(q):
+    lv = q.levels.cpu().numpy()
+    pa = q.parents.cpu().numpy()
+    wl, wp = alone[(q.graph, q.root)]
+    checked.append(np.array_equal(lv, wl) and np.array_equal(pa, wp))
+
+  budget = 40 * 8 * max(a.n for a in arrays.values())
+  srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget, on_done=on_done)
+  orig = srv._buffers
+
+  def tracked(name):
+    peak[0] = max(peak[0], srv.in_use + srv._bytes(name))
+    return orig(name)
+  srv._buffers = tracked
+  rep = srv.run(arrivals, realtime=True)
+  srv.close()
+  assert len(rep.queries) == 300 and all(checked) and len(checked) == 300
+  assert srv.in_use == 0 and peak[0] <= budget + 8 * max(a.n for a in arrays.values())
+  s = rep.summary()
+  assert s["p99_ms"] >= s["p50_ms"] > 0
+  base = serving.serial_baseline(graphs, arrivals, realtime=False)
+  assert len(base.queries) == 300
+  for g in graphs.values():
+    g.close()
