@@ -95,6 +95,8 @@ struct MsParams {
   uint32_t *bigoff0, *bigoff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
   const int32_t *hub_vtx;    // [nhub]
+  const int32_t *med_vtx;    // [nmed] vertices of in-degree in (kPullLight, kHubDeg]
+  int64_t nmed;
   const uint32_t *hub_choff; // [nhub + 1] prefix of in-list chunks
   uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
   uint64_t *hub_found;       // [nhub][W] lanes found this round
@@ -478,6 +480,7 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   const int next_parity = (L + 1) & 1;
   int32_t *q = next_parity ? p.queue1 : p.queue0;
   uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
+  // light vertices (in-degree <= kPullLight): one thread each
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
        base < p.n; base += nthreads) {
     const int64_t v = base + lane_id();
@@ -490,11 +493,12 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       if (want.any()) {
         s = __ldg(p.in_off + v);
         e = __ldg(p.in_off + v + 1);
-        if (e - s > kHubDeg) want = Mask<W>::zero();  // a hub: done by chunks
+        if (e - s > kPullLight) want = Mask<W>::zero();  // medium list or hub chunks
       }
     }
     if (!__ballot_sync(kMsFull, want.any())) continue;
-    const Mask<W> got = scan_group<W>(p, v, s, e, want, cur, L);
+    Mask<W> got = Mask<W>::zero();
+    if (want.any()) got = thread_scan<W>(p, v, s, e, want, cur, L);
     bool claimed = false;
     int64_t deg = 0;
     if (got.any()) {
@@ -506,6 +510,26 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
     }
     ms_enqueue(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+  }
+  // medium vertices (kPullLight < in-degree <= kHubDeg, a fixed list): one warp each
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = warp_id_global(); j < p.nmed; j += nwarps) {
+    const int32_t v = p.med_vtx[j];
+    const Mask<W> seen = ld_mask<W>(p.vis, v);
+    const Mask<W> want = active.andnot(seen);
+    if (!want.any()) continue;
+    const Mask<W> got = warp_scan<W>(p, v, __ldg(p.in_off + v), __ldg(p.in_off + v + 1), want,
+                                     cur, L, -1);
+    const bool claimed = lane_id() == 0 && got.any();
+    int64_t deg = 0;
+    if (claimed) {
+      st_mask<W>(nxt, v, got);
+      st_mask<W>(p.vis, v, seen | got);
+      acc.visits += (unsigned long long)got.popc();
+      acc_lanes<W>(acc, got);
+      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+    }
+    ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
   if (p.nhub > 0) hub_chunks<W>(p, cur, active, L);
 }
@@ -631,14 +655,17 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
   const unsigned nbig = (unsigned)(bigw >> 32), big_edges = (unsigned)bigw;
   const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
-  const unsigned nb = (big_edges + kPushChunk - 1) / kPushChunk;
+  // chunks of 32 .. kPushChunk edges: small frontiers still spread over the grid
+  unsigned chunk = ((big_edges / (unsigned)nwarps) + 31u) & ~31u;
+  chunk = chunk < 32u ? 32u : (chunk > (unsigned)kPushChunk ? (unsigned)kPushChunk : chunk);
+  const unsigned nb = (big_edges + chunk - 1) / chunk;
   const unsigned nitems = nb + (nlight + 31u) / 32u;
   unsigned item = (unsigned)warp_id_global();
   while (item < nitems) {
     if (item < nb) {
-      const unsigned x0 = item * kPushChunk;
-      ms_push_chunk<W>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0,
-                       min(x0 + (unsigned)kPushChunk, big_edges), qn, bn, Rn, acc);
+      const unsigned x0 = item * chunk;
+      ms_push_chunk<W>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0, min(x0 + chunk, big_edges),
+                       qn, bn, Rn, acc);
     } else {
       const unsigned idx = (item - nb) * 32u + lane;
       int32_t u = -1;
@@ -701,21 +728,23 @@ __device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, uint64
   const int64_t nl = *(volatile unsigned *)&Rn->res_light;
   const int64_t nbg = *(volatile unsigned *)&Rn->res_big;
   const int64_t total = nl + nbg;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total;
-       base += nthreads) {
-    const int64_t j = base + lane_id();
-    int64_t v = 0, s = 0, e = 0;
-    Mask<W> nw = Mask<W>::zero();
-    if (j < total) {
-      v = j < nl ? q[j] : q[p.n - 1 - (j - nl)];
-      nw = ld_mask<W>(nxt, v);
-      st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
-      acc.visits += (unsigned long long)nw.popc();
-      acc_lanes<W>(acc, nw);
-      s = __ldg(p.in_off + v);
-      e = __ldg(p.in_off + v + 1);
-    }
-    scan_group<W>(p, v, s, e, nw, cur, L);
+  // every entry: merge into vis; short in-lists scanned by their thread
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += nthreads) {
+    const int64_t v = j < nl ? q[j] : q[p.n - 1 - (j - nl)];
+    const Mask<W> nw = ld_mask<W>(nxt, v);
+    st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
+    acc.visits += (unsigned long long)nw.popc();
+    acc_lanes<W>(acc, nw);
+    const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+    if (e - s <= kPullLight) thread_scan<W>(p, v, s, e, nw, cur, L);
+  }
+  // longer in-lists: one warp per entry
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = warp_id_global(); j < total; j += nwarps) {
+    const int64_t v = j < nl ? q[j] : q[p.n - 1 - (j - nl)];
+    const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+    if (e - s <= kPullLight) continue;
+    warp_scan<W>(p, v, s, e, ld_mask<W>(nxt, v), cur, L, -1);
   }
   if (p.nhub > 0) hub_finalize<W>(p, L, nxt, Rn, acc);
 }
@@ -1005,8 +1034,10 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
 
 // ---------------------------------------------------------------------------
 // per-graph hub list: vertices of in-degree > kHubDeg, their chunk prefix
+// per-graph vertex lists by in-degree: hubs (> kHubDeg) with their slot map,
+// and medium vertices (kPullLight, kHubDeg]
 __global__ void hub_mark_kernel(int64_t n, const int64_t *__restrict__ in_off, int32_t *hub_slot,
-                                int32_t *hub_vtx, unsigned *count) {
+                                int32_t *hub_vtx, int32_t *med_vtx, unsigned *count) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     const int64_t d = in_off[v + 1] - in_off[v];
@@ -1014,6 +1045,8 @@ __global__ void hub_mark_kernel(int64_t n, const int64_t *__restrict__ in_off, i
     if (d > kHubDeg) {
       slot = (int32_t)atomicAdd(count, 1u);
       hub_vtx[slot] = (int32_t)v;
+    } else if (d > kPullLight) {
+      med_vtx[atomicAdd(count + 1, 1u)] = (int32_t)v;
     }
     hub_slot[v] = slot;
   }
@@ -1034,6 +1067,8 @@ struct MsState {
   uint32_t *bigoff = nullptr;
   int32_t *hub_slot = nullptr;
   int32_t *hub_vtx = nullptr;
+  int32_t *med_vtx = nullptr;
+  int64_t nmed = 0;
   uint32_t *hub_choff = nullptr;
   uint32_t *hub_cand = nullptr;
   uint64_t *hub_found = nullptr;
@@ -1051,6 +1086,7 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->bigoff);
   cudaFree(s->hub_slot);
   cudaFree(s->hub_vtx);
+  cudaFree(s->med_vtx);
   cudaFree(s->hub_choff);
   cudaFree(s->hub_cand);
   cudaFree(s->hub_found);
@@ -1072,26 +1108,31 @@ int64_t bfs_big_capacity(int64_t n, int64_t nnz);
 
 static int ms_build_hubs(cg_graph *g, MsState *s) {
   const int64_t cap = g->nnz / (kHubDeg + 1) + 1;
+  int64_t mcap = g->nnz / (kPullLight + 1) + 1;
+  if (mcap > g->n) mcap = g->n;
   unsigned *d_count = nullptr;
   if (cudaMalloc(&s->hub_slot, sizeof(int32_t) * (size_t)g->n) != cudaSuccess ||
       cudaMalloc(&s->hub_vtx, sizeof(int32_t) * (size_t)cap) != cudaSuccess ||
-      cudaMalloc(&d_count, sizeof(unsigned)) != cudaSuccess) {
+      cudaMalloc(&s->med_vtx, sizeof(int32_t) * (size_t)mcap) != cudaSuccess ||
+      cudaMalloc(&d_count, 2 * sizeof(unsigned)) != cudaSuccess) {
     cudaFree(d_count);
     return CG_ERR_OUT_OF_MEMORY;
   }
   int rc = CG_OK;
   do {
-    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned), g->stream);
+    cudaError_t e = cudaMemsetAsync(d_count, 0, 2 * sizeof(unsigned), g->stream);
     if (e != cudaSuccess) { rc = cuda_fail(e, "hub count"); break; }
     int blocks = (int)((g->n + 255) / 256);
     if (blocks > g->num_sms * 16) blocks = g->num_sms * 16;
     hub_mark_kernel<<<blocks, 256, 0, g->stream>>>(g->n, g->in_off, s->hub_slot, s->hub_vtx,
-                                                    d_count);
-    unsigned nhub = 0;
-    e = cudaMemcpyAsync(&nhub, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+                                                    s->med_vtx, d_count);
+    unsigned counts[2] = {0u, 0u};
+    e = cudaMemcpyAsync(counts, d_count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) { rc = cuda_fail(e, "hub mark"); break; }
+    const unsigned nhub = counts[0];
     s->nhub = (int)nhub;
+    s->nmed = counts[1];
     const size_t nh = nhub > 0 ? nhub : 1;
     if (cudaMalloc(&s->hub_choff, sizeof(uint32_t) * (nh + 1)) != cudaSuccess ||
         cudaMalloc(&s->hub_cand, sizeof(uint32_t) * nh * 64 * s->lane_words) != cudaSuccess ||
@@ -1120,7 +1161,7 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
     delete[] h_chunks;
     cudaFree(chunks);
     if (e != cudaSuccess) { rc = cuda_fail(e, "hub chunks"); break; }
-    g->device_bytes += sizeof(int32_t) * g->n + sizeof(int32_t) * cap +
+    g->device_bytes += sizeof(int32_t) * g->n + sizeof(int32_t) * (cap + mcap) +
                        nh * (sizeof(uint32_t) * (1 + 64 * s->lane_words + 4) +
                              sizeof(uint64_t) * s->lane_words);
   } while (0);
@@ -1211,6 +1252,8 @@ static MsParams ms_params(const cg_graph *g, const MsState *s) {
   const int64_t nh = s->nhub > 0 ? s->nhub : 1;
   p.hub_slot = s->hub_slot;
   p.hub_vtx = s->hub_vtx;
+  p.med_vtx = s->med_vtx;
+  p.nmed = s->nmed;
   p.hub_choff = s->hub_choff;
   p.hub_cand = s->hub_cand;
   p.hub_found = s->hub_found;
