@@ -19,6 +19,15 @@ CG_ERR_LEVEL_CAP = 4
 CG_ERR_TIMEOUT = 5
 CG_ERR_NOT_SUPPORTED = 6
 CG_ERR_ADMISSION = 7
+CG_ERR_PARSE = 8
+CG_ERR_IO = 9
+
+CG_EDGES_SYMMETRIZE = 1
+CG_EDGES_DROP_LOOPS = 2
+CG_EDGES_DETECT_SYMMETRIC = 4
+
+CG_FORMAT_MTX = 1
+CG_FORMAT_EDGELIST = 2
 
 CG_DIR_AUTO = 0
 CG_DIR_TOPDOWN = 1
@@ -63,12 +72,32 @@ class CgStats(ctypes.Structure):
             "finish_ns": self.finish_ns}
 
 
+class CgEdgeList(ctypes.Structure):
+  _fields_ = [("n", ctypes.c_int64), ("m", ctypes.c_int64),
+              ("src", ctypes.POINTER(ctypes.c_uint32)), ("dst", ctypes.POINTER(ctypes.c_uint32)),
+              ("format", ctypes.c_int32), ("mtx_symmetry", ctypes.c_int32)]
+
+
+CG_CHECK_NAMES = ("root", "tree", "edges", "span", "tree_edge", "lowest")
+
+
+class CgValidation(ctypes.Structure):
+  _fields_ = [("failures", ctypes.c_int64 * 6), ("first", ctypes.c_int64 * 6)]
+
+  def as_dict(self):
+    return {name: {"failures": int(self.failures[i]), "first": int(self.first[i])}
+            for i, name in enumerate(CG_CHECK_NAMES)}
+
+  def ok(self, lowest=True):
+    return all(self.failures[i] == 0 for i in range(6) if lowest or i != 5)
+
+
 class CgError(RuntimeError):
   def __init__(self, status, what=""):
     self.status = status
     msg = f"{what}: {strerror(status)} ({status})"
     detail = last_error_string()
-    if status == CG_ERR_CUDA and detail:
+    if status in (CG_ERR_CUDA, CG_ERR_PARSE, CG_ERR_IO, CG_ERR_NOT_SUPPORTED) and detail:
       msg += f" -- {detail}"
     super().__init__(msg)
 
@@ -102,6 +131,14 @@ SIGNATURES = {
     "cg_graph_from_edges": ([ctypes.c_int64, ctypes.c_int64, _P, _P, ctypes.c_int32,
                              ctypes.POINTER(_P)], ctypes.c_int),
     "cg_graph_export": ([_P, _P, _P, _P, _P], ctypes.c_int),
+    "cg_parse_edges": ([ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32,
+                        ctypes.POINTER(CgEdgeList)], ctypes.c_int),
+    "cg_edge_list_free": ([ctypes.POINTER(CgEdgeList)], ctypes.c_int),
+    "cg_graph_from_text": ([ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(_P)],
+                           ctypes.c_int),
+    "cg_graph_load": ([ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(_P)], ctypes.c_int),
+    "cg_validate_device": ([_P, _P, ctypes.c_int32, _P, _P, ctypes.POINTER(CgValidation)],
+                           ctypes.c_int),
     "cg_bfs_noalloc": ([ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P, ctypes.c_int64, _P, _P,
                         ctypes.POINTER(CgStats), _P], ctypes.c_int),
     "cg_pool_create": ([_P, ctypes.c_int32, ctypes.POINTER(_P)], ctypes.c_int),

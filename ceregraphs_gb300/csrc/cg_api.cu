@@ -87,6 +87,8 @@ const char *cg_strerror(int status) {
     case CG_ERR_TIMEOUT: return "device-side wait timed out";
     case CG_ERR_NOT_SUPPORTED: return "not supported on this device";
     case CG_ERR_ADMISSION: return "request exceeds the HBM budget";
+    case CG_ERR_PARSE: return "malformed graph file";
+    case CG_ERR_IO: return "graph file could not be read";
     default: return "unknown status";
   }
 }

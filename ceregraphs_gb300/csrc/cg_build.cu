@@ -164,6 +164,19 @@ __global__ void csr_from_keys_kernel(int64_t n, int64_t nnz, const uint64_t *__r
   }
 }
 
+// A == A^T exactly when the CSR and the CSC of the same entries coincide.
+__global__ void same_arrays_kernel(int64_t n, int64_t nnz, const int64_t *__restrict__ a_off,
+                                   const int32_t *__restrict__ a_idx,
+                                   const int64_t *__restrict__ b_off,
+                                   const int32_t *__restrict__ b_idx, unsigned *differ) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool d = false;
+  for (int64_t i = t0; i < nnz; i += stride) d |= a_idx[i] != b_idx[i];
+  for (int64_t r = t0; r <= n; r += stride) d |= a_off[r] != b_off[r];
+  if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) atomicOr(differ, 1u);
+}
+
 static int grid_for(int64_t work, int num_sms) {
   int64_t b = (work + 255) / 256;
   const int64_t cap = (int64_t)num_sms * 32;
@@ -268,6 +281,8 @@ int cg_graph_from_edges(int64_t n, int64_t m, const uint32_t *d_src, const uint3
   *out = nullptr;
   const bool sym = (flags & CG_EDGES_SYMMETRIZE) != 0;
   const bool drop = (flags & CG_EDGES_DROP_LOOPS) != 0;
+  const bool detect = (flags & CG_EDGES_DETECT_SYMMETRIC) != 0;
+  bool found_sym = false;
   int dev = 0, sms = 0;
   CG_CUDA(cudaGetDevice(&dev));
   CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -326,13 +341,29 @@ int cg_graph_from_edges(int64_t n, int64_t m, const uint32_t *d_src, const uint3
                                                                                 out_off, out_idx);
       e = cudaGetLastError();
       if (e != cudaSuccess) { rc = cuda_fail(e, "csc_from_keys"); break; }
+      if (detect) {
+        // the key buffers are free now: borrow one word of `keys` for the flag
+        unsigned *differ = reinterpret_cast<unsigned *>(keys);
+        e = cudaMemsetAsync(differ, 0, sizeof(unsigned), st);
+        if (e == cudaSuccess) {
+          same_arrays_kernel<<<grid_for(nnz > n ? nnz : n + 1, sms), 256, 0, st>>>(
+              n, nnz, in_off, in_idx, out_off, out_idx, differ);
+          e = cudaGetLastError();
+        }
+        unsigned h_differ = 1u;
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(&h_differ, differ, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "symmetry check"); break; }
+        found_sym = h_differ == 0u;
+      }
     }
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { rc = cuda_fail(e, "cg_graph_from_edges"); break; }
     cudaFree(keys);
     cudaFree(tmp);
     keys = tmp = nullptr;
-    const bool out_sym = sym || nnz == 0;
+    const bool out_sym = sym || nnz == 0 || found_sym;
     rc = cg_graph_create(n, nnz, in_off, in_idx, out_sym ? nullptr : out_off,
                          out_sym ? nullptr : out_idx,
                          CG_GRAPH_DEVICE_PTRS | (out_sym ? CG_GRAPH_SYMMETRIC : 0), out);

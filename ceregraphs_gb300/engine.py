@@ -239,6 +239,19 @@ class Graph:
     check(rc, "cg_capture_end")
     return Exec(x)
 
+  def validate(self, roots, d_levels, d_parents):
+    """Graph500 tree checks on the device for searches whose outputs are
+    device tensors (k x n, or n for one search).  Returns one dict per search:
+    check name -> {"failures", "first"}; see cg_validate_device."""
+    roots = np.ascontiguousarray(np.atleast_1d(roots), dtype=np.int64)
+    k = len(roots)
+    out = (_lib.CgValidation * k)()
+    lp = d_levels if isinstance(d_levels, int) else d_levels.data_ptr()
+    pp = d_parents if isinstance(d_parents, int) else d_parents.data_ptr()
+    check(_lib.load().cg_validate_device(self._h, _ptr(roots), k, ctypes.c_void_p(lp),
+                                         ctypes.c_void_p(pp), out), "cg_validate_device")
+    return [out[i].as_dict() for i in range(k)]
+
   def count_edges(self, d_levels, k=1):
     """Graph500 m for k searches whose levels are on the device (k x n)."""
     lp = d_levels if isinstance(d_levels, int) else d_levels.data_ptr()

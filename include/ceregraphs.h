@@ -42,7 +42,9 @@ typedef enum cg_status {
   CG_ERR_LEVEL_CAP = 4,     /* the search ran more rounds than the cap allows */
   CG_ERR_TIMEOUT = 5,       /* a device-side wait ran out; the context stays usable */
   CG_ERR_NOT_SUPPORTED = 6, /* e.g. cooperative launch unavailable */
-  CG_ERR_ADMISSION = 7      /* refused: the request does not fit the HBM budget */
+  CG_ERR_ADMISSION = 7,     /* refused: the request does not fit the HBM budget */
+  CG_ERR_PARSE = 8,         /* malformed graph file; the line is in cg_last_error_string */
+  CG_ERR_IO = 9             /* a graph file could not be read */
 } cg_status;
 
 typedef struct cg_graph cg_graph;
@@ -209,7 +211,8 @@ int cg_uniform_bits(const uint64_t *gen_state, uint64_t first, int64_t count, in
 /* Edge-list flags for cg_graph_from_edges. */
 enum {
   CG_EDGES_SYMMETRIZE = 1,  /* store both directions (gen_rmat.py:34-36) */
-  CG_EDGES_DROP_LOOPS = 2   /* drop self-loops (gen_rmat.py:37-38) */
+  CG_EDGES_DROP_LOOPS = 2,  /* drop self-loops (gen_rmat.py:37-38) */
+  CG_EDGES_DETECT_SYMMETRIC = 4 /* keep one copy when A == A^T (run_graph500.py:179) */
 };
 
 /* Kernel 1 from a device edge list src[e] -> dst[e] (entries A[dst, src]):
@@ -222,6 +225,63 @@ int cg_graph_from_edges(int64_t n, int64_t m, const uint32_t *d_src, const uint3
  * (n+1 int64) and indices (nnz int32), CSC likewise. */
 int cg_graph_export(const cg_graph *g, int64_t *in_off, int32_t *in_idx, int64_t *out_off,
                     int32_t *out_idx);
+
+/* ---- graph files -----------------------------------------------------------
+ * Replaces graph_loader.load_graph (bfs/implementation/graph_loader.py:27-95)
+ * with the reference's format detection and direction rule:
+ *  - Matrix Market (first line starts with "%%MatrixMarket"), coordinate
+ *    storage: entry (i, j), 1-based, is A[i-1, j-1], the edge j-1 -> i-1;
+ *    symmetric / skew-symmetric / hermitian storage is mirrored off the
+ *    diagonal (scipy.io.mmread); values are ignored (the reference consumes
+ *    indptr/indices only); rows must equal cols.
+ *  - otherwise a SNAP edge list: "u v" per line (whitespace separated, extra
+ *    columns ignored) is the edge u -> v, i.e. A[v, u] (graph_loader.py:78-93);
+ *    '#' lines are comments, except that "Nodes: N" in one declares the vertex
+ *    count; n = max(N, max id + 1).
+ * Compressed files are decompressed by the caller (the Python loader handles
+ * .gz and .bz2). */
+enum { CG_FORMAT_MTX = 1, CG_FORMAT_EDGELIST = 2 };
+typedef struct cg_edge_list {
+  int64_t n;             /* vertices */
+  int64_t m;             /* edges, symmetric storage expanded, duplicates kept */
+  uint32_t *src;         /* host arrays of m, owned by the library */
+  uint32_t *dst;
+  int32_t format;        /* CG_FORMAT_* */
+  int32_t mtx_symmetry;  /* 0 general, 1 symmetric, 2 skew-symmetric, 3 hermitian */
+} cg_edge_list;
+/* Parses `len` bytes of text with up to `threads` host threads (<= 0: all
+ * cores).  Host-only: needs no GPU.  Free the result with cg_edge_list_free. */
+int cg_parse_edges(const char *text, int64_t len, int32_t threads, cg_edge_list *out);
+int cg_edge_list_free(cg_edge_list *el);
+/* Kernel 1 from graph text: parse on the host, then the device build of
+ * cg_graph_from_edges with CG_EDGES_DETECT_SYMMETRIC added to `flags`. */
+int cg_graph_from_text(const char *text, int64_t len, int32_t flags, cg_graph **out);
+/* The same from an uncompressed file (CG_ERR_IO if it cannot be read). */
+int cg_graph_load(const char *path, int32_t flags, cg_graph **out);
+
+/* ---- result validation on the device --------------------------------------
+ * The Graph500 tree checks for k searches whose levels and parents (k x n,
+ * search-major, -1 = unreached) are in device memory, in two passes over the
+ * resident graph.  Replaces the per-search host cross-check of
+ * run_graph500.py:383-395 and bfs/plots/bfs_tree_plot.py:140-152.  out[i]
+ * counts the failing vertices of search i per check, and the lowest one
+ * (-1 if none).  Values are treated as untrusted (never dereferenced out of
+ * range). */
+enum {
+  CG_CHECK_ROOT = 0,      /* parent[root] == root, level[root] == 0 */
+  CG_CHECK_TREE = 1,      /* reached v != root: level[parent[v]] == level[v] - 1 */
+  CG_CHECK_EDGES = 2,     /* edge u -> v, u reached: v reached, level[v] <= level[u] + 1 */
+  CG_CHECK_SPAN = 3,      /* level[v] >= 0 exactly when parent[v] >= 0 */
+  CG_CHECK_TREE_EDGE = 4, /* parent[v] -> v is an input edge */
+  CG_CHECK_LOWEST = 5,    /* parent[v] is the lowest in-neighbour one level up */
+  CG_CHECKS = 6
+};
+typedef struct cg_validation {
+  int64_t failures[CG_CHECKS];
+  int64_t first[CG_CHECKS];
+} cg_validation;
+int cg_validate_device(cg_graph *g, const int64_t *roots, int32_t k, const int32_t *d_levels,
+                       const int32_t *d_parents, cg_validation *out);
 
 /* ---- one search without any library allocation --------------------------
  * No counterpart in the reference.  For callers that cannot let this library

@@ -207,6 +207,9 @@ def graph500_validate(A_csr, source, levels, parent):
     errs.append("1: parent pointers do not all lead to the root (cycle or break)")
   # 2. tree edges span one level
   ch = np.where(reached & (np.arange(n) != source))[0]
+  if np.any(parent[ch] >= n):
+    errs.append("1: a parent is out of range")
+    ch = ch[parent[ch] < n]
   if np.any(levels[parent[ch]] != levels[ch] - 1):
     errs.append("2: a tree edge does not join consecutive levels")
   # 3. graph edges (c -> r) span at most one level among reached vertices;
@@ -230,6 +233,65 @@ def graph500_validate(A_csr, source, levels, parent):
     if np.any(np.asarray(A[ch, parent[ch]]).reshape(-1) == 0):
       errs.append("5: a tree edge is not an input edge")
   return errs
+
+
+CHECKS = ("root", "tree", "edges", "span", "tree_edge", "lowest")
+
+
+def validation_counts(in_off, in_idx, root, levels, parents):
+  """The per-check tallies of the device validator, restated in numpy:
+  {check: (failures, lowest failing vertex or -1)}.
+
+  The checks are graph500_validate's (above) written per vertex, plus the
+  lowest-index parent rule of bfs/README.md:208-224: root (parent[root] ==
+  root at level 0), tree (a reached v != root has a parent in range one level
+  up), edges (per stored entry u -> v: u reached implies v reached no deeper
+  than level[u] + 1 -- counted per entry), span (levels and parents agree on
+  the reached set), tree_edge (parent[v] -> v is an input edge,
+  bfs_tree_plot.py:140-152) and lowest (parent[v] is the lowest in-neighbour
+  one level up).  tree_edge and lowest are only asked of vertices that pass
+  tree.
+  """
+  in_off = np.asarray(in_off, dtype=np.int64)
+  in_idx = np.asarray(in_idx, dtype=np.int64)
+  lv = np.asarray(levels, dtype=np.int64)
+  pa = np.asarray(parents, dtype=np.int64)
+  n = len(in_off) - 1
+  v = np.arange(n)
+  rows = np.repeat(v, np.diff(in_off))
+  out = {}
+
+  def put(name, bad_mask):
+    idx = np.nonzero(bad_mask)[0]
+    out[name] = (int(len(idx)), int(idx[0]) if len(idx) else -1)
+
+  put("span", (lv >= 0) != (pa >= 0))
+  put("root", (v == root) & ((pa != root) | (lv != 0)))
+  cand = (v != root) & (pa >= 0)
+  in_range = cand & (pa < n)
+  lp = np.where(in_range, lv[np.clip(pa, 0, n - 1)], -2)
+  tree_bad = (cand & ((pa >= n) | (lv < 1) | (lp != lv - 1))) | ((v != root) & (pa < -1))
+  put("tree", tree_bad)
+  ok = cand & ~tree_bad
+  keys = rows * n + in_idx                      # sorted: rows ascending, in-lists sorted
+  want = v * n + np.where(ok, pa, 0)
+  pos = np.searchsorted(keys, want)
+  has = (pos < len(keys)) & (keys[np.minimum(pos, len(keys) - 1)] == want) if len(keys) else \
+      np.zeros(n, dtype=bool)
+  put("tree_edge", ok & ~has)
+  lu = lv[in_idx]
+  hit = lu == lv[rows] - 1
+  low = np.full(n, -1, dtype=np.int64)
+  big = np.iinfo(np.int64).max
+  first = np.full(n, big, dtype=np.int64)
+  np.minimum.at(first, rows[hit], in_idx[hit])
+  low = np.where(first == big, -1, first)
+  put("lowest", ok & (low != pa))
+  lr = lv[rows]
+  ebad = (lu >= 0) & ((lr < 0) | (lr > lu + 1))
+  cnt = int(ebad.sum())
+  out["edges"] = (cnt, int(rows[ebad].min()) if cnt else -1)
+  return out
 
 
 # --------------------------------------------------------------------------

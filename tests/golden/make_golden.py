@@ -129,6 +129,49 @@ def search_record(A, source, is_symmetric, bfs_timing, device_io, bfs_tree_plot,
   return rec
 
 
+# Graph files for the loader, each read by the reference's load_graph
+# (graph_loader.py:27-95): format detection, the (dst, src) rule, "Nodes:"
+# declarations, Python's universal newlines, mmread's symmetric expansion.
+LOADER_CASES = {
+    "snap": ("tiny.txt",
+             "# Directed graph\n# Nodes: 7 Edges: 6\n0\t1\n0\t2\n2\t3\n3\t0\n4\t5\n5 5\n"),
+    "snap_crlf_extra_columns": ("crlf.txt",
+                                "# Nodes: 10\r\n1 2 0.5 x\r\n\r\n  3\t4  \r\n2 1\r\n9 0\r\n"),
+    "snap_cr_only": ("cr.txt", "0 1\r1 2\r# c\r2 0\r"),
+    "snap_declared_too_small": ("small.txt", "# Nodes: 3\n0 5\n5 0\n"),
+    "snap_duplicates_and_loops": ("dup.txt", "1 1\n1 2\n1 2\n2 1\n# Nodes:   4 Edges: 9\n"),
+    "snap_gzip": ("g.txt.gz", "# Nodes: 6\n0 1\n1 2\n2 3\n3 4\n4 5\n5 0\n"),
+    "mtx": ("tiny.mtx", "%%MatrixMarket matrix coordinate real general\n% tiny\n5 5 6\n"
+                        "1 2 1.0\n2 1 1.0\n2 3 1.0\n3 2 1.0\n4 5 1.0\n5 4 1.0\n"),
+    "mtx_pattern_symmetric": ("sym.mtx", "%%MatrixMarket matrix coordinate pattern symmetric\n"
+                                         "% c1\n%c2\n6 6 5\n2 1\n3 1\n3 3\n6 4\n5 2\n"),
+    "mtx_integer_skew": ("skew.mtx", "%%MatrixMarket matrix coordinate integer skew-symmetric\n"
+                                     "4 4 3\n2 1 5\n3 2 -1\n4 1 7\n"),
+    "mtx_duplicates_zero": ("dupz.mtx", "%%MatrixMarket matrix coordinate real general\n"
+                                        "3 3 4\n1 2 0.0\n1 2 1.5\n3 1 2\n3 3 0\n"),
+}
+
+
+def loader_cases(graph_loader):
+  import gzip
+  cases = {}
+  with tempfile.TemporaryDirectory() as td:
+    for name, (fname, text) in LOADER_CASES.items():
+      path = os.path.join(td, fname)
+      if fname.endswith(".gz"):
+        with gzip.open(path, "wb") as f:
+          f.write(text.encode())
+      else:
+        with open(path, "w", encoding="utf-8", newline="") as f:
+          f.write(text)
+      M = sparse.csr_matrix(graph_loader.load_graph(path))
+      M.sum_duplicates()
+      M.sort_indices()
+      cases[name] = {"file": fname, "text": text, "shape": list(M.shape),
+                     "indptr": M.indptr.tolist(), "indices": M.indices.tolist()}
+  return cases
+
+
 def main(ref):
   gen_rmat, bfs_timing, device_io, graph_loader, bfs_tree_plot, rg = import_reference(ref)
   out = {"graphs": {}, "searches": {}, "pick_sources": {}, "harmonic_mean": [],
@@ -229,30 +272,7 @@ def main(ref):
       "planted": p.tolist(),
       "bad": [int(x) for x in bfs_tree_plot.invalid_parents(p, visited, A, 0)]}
 
-  # --- loader: SNAP edge list -> (dst, src) ---
-  with tempfile.TemporaryDirectory() as td:
-    path = os.path.join(td, "tiny.txt")
-    text = "# Directed graph\n# Nodes: 7 Edges: 6\n0\t1\n0\t2\n2\t3\n3\t0\n4\t5\n5 5\n"
-    with open(path, "w", encoding="utf-8") as f:
-      f.write(text)
-    L = graph_loader.load_graph(path).tocsr()
-    L.sum_duplicates()
-    L.sort_indices()
-    out["loader"]["snap_text"] = text
-    out["loader"]["snap_shape"] = list(L.shape)
-    out["loader"]["snap_indptr"] = L.indptr.tolist()
-    out["loader"]["snap_indices"] = L.indices.tolist()
-    mpath = os.path.join(td, "tiny.mtx")
-    mtext = ("%%MatrixMarket matrix coordinate real general\n% tiny\n5 5 6\n"
-             "1 2 1.0\n2 1 1.0\n2 3 1.0\n3 2 1.0\n4 5 1.0\n5 4 1.0\n")
-    with open(mpath, "w", encoding="utf-8") as f:
-      f.write(mtext)
-    M = sparse.csr_matrix(graph_loader.load_graph(mpath))
-    M.sort_indices()
-    out["loader"]["mtx_text"] = mtext
-    out["loader"]["mtx_shape"] = list(M.shape)
-    out["loader"]["mtx_indptr"] = M.indptr.tolist()
-    out["loader"]["mtx_indices"] = M.indices.tolist()
+  out["loader"] = loader_cases(graph_loader)
 
   with open(os.path.join(HERE, "golden.json"), "w", encoding="utf-8") as f:
     json.dump(out, f, indent=1, sort_keys=True)
@@ -260,5 +280,22 @@ def main(ref):
   print("wrote golden.json and golden_arrays.npz")
 
 
+def main_loader_only(ref):
+  """Refresh only the loader section of golden.json."""
+  mods = import_reference(ref)
+  path = os.path.join(HERE, "golden.json")
+  with open(path, encoding="utf-8") as f:
+    out = json.load(f)
+  out["loader"] = loader_cases(mods[3])
+  with open(path, "w", encoding="utf-8") as f:
+    json.dump(out, f, indent=1, sort_keys=True)
+  print("refreshed the loader section of golden.json")
+
+
 if __name__ == "__main__":
-  main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+  args = [a for a in sys.argv[1:] if not a.startswith("--")]
+  ref_dir = args[0] if args else "/root/reference"
+  if "--loader-only" in sys.argv:
+    main_loader_only(ref_dir)
+  else:
+    main(ref_dir)

@@ -145,3 +145,22 @@ def test_grid_csr_is_sorted_and_symmetric():
   for v in range(a.n):
     row = a.in_idx[a.in_off[v]:a.in_off[v + 1]]
     assert np.all(np.diff(row) > 0)
+
+
+def test_driver_csv_header_guard(tmp_path):
+  from ceregraphs_gb300 import run_graph500
+  p = tmp_path / "s.csv"
+  run_graph500.append_csv(str(p), [{"a": 1, "b": 2}])
+  run_graph500.append_csv(str(p), [{"a": 3, "b": 4}])
+  assert p.read_text().splitlines() == ["a,b", "1,2", "3,4"]
+  with pytest.raises(SystemExit):
+    run_graph500.append_csv(str(p), [{"a": 1, "c": 2}])
+
+
+def test_driver_arguments():
+  from ceregraphs_gb300 import run_graph500
+  a = run_graph500.parse_args(["--rmat", "12", "16", "0", "--mode", "batched", "--lanes", "128"])
+  assert a.rmat == [12, 16, 0] and a.mode == "batched" and a.lanes == 128
+  assert a.num_searches == 64 and not a.nocorrectness
+  with pytest.raises(SystemExit):
+    run_graph500.parse_args(["--num-searches", "3"])   # a graph source is required
