@@ -46,7 +46,7 @@ class CgOptions(ctypes.Structure):
               ("block_size", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
               ("level_cap", ctypes.c_int32), ("wait_timeout_ms", ctypes.c_int32),
               ("lane_words", ctypes.c_int32), ("ms_alpha", ctypes.c_float),
-              ("test_unmatched_wait", ctypes.c_int32)]
+              ("test_unmatched_wait", ctypes.c_int32), ("ms_history", ctypes.c_int32)]
 
   def as_dict(self):
     return {k: getattr(self, k) for k, _ in self._fields_}

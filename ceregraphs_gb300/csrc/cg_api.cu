@@ -109,6 +109,7 @@ void cg_default_options(cg_options *opt) {
   opt->lane_words = 1;
   opt->ms_alpha = 4.f;
   opt->test_unmatched_wait = 0;
+  opt->ms_history = 0;
 }
 
 int cg_graph_create(int64_t n, int64_t nnz, const int64_t *in_off, const int32_t *in_idx,

@@ -34,179 +34,9 @@
 
 #include <new>
 
-#include "cg_internal.cuh"
+#include "cg_ms.cuh"
 
 namespace cg {
-
-constexpr unsigned kMsFull = 0xffffffffu;
-constexpr int kMsBlock = 512;
-constexpr int kMsMaxLanes = 128;
-constexpr int kPullLight = 32;    // in-degree <= this: one thread scans the in-list
-constexpr int kHubDeg = 1024;     // in-degree > this: hub
-constexpr int kHubChunk = 1024;   // in-list entries of a hub per work item
-
-struct MsRound {
-  unsigned long long nf[kCounterShards];      // vertices with a nonzero frontier mask
-  unsigned long long visits[kCounterShards];  // lane discoveries
-  unsigned long long mf[kCounterShards];      // sum of out-degrees over the frontier
-  unsigned long long big;       // queue: (count << 32) | edges of its big vertices
-  unsigned int nlight, work;
-  unsigned int res_light, res_big;  // queue counts a push round's resolve phase covers
-  unsigned long long lanes[2];  // lanes whose frontier is non-empty
-  unsigned long long pad[2];
-};
-
-// Lane table of a serving pool: where each lane's outputs go and the round at
-// which its search started (its level = round + 1 - start).
-struct LaneTable {
-  int32_t *levels[kMsMaxLanes];
-  int32_t *parents[kMsMaxLanes];
-  int32_t start[kMsMaxLanes];
-};
-
-// Only the block that arrives last at a round's grid-wide wait touches the
-// round bookkeeping (L .. t_round); the waits order those accesses.  L and
-// dir persist between launches, so a serving pool resumes where it stopped.
-struct MsCtl {
-  GridWait wait;
-  int status;
-  int L;                          // next round to run
-  int dir;                        // its direction (0 push, 1 pull)
-  int pull_rounds;
-  int switches;
-  int pad0;
-  unsigned long long visited;
-  unsigned long long done[2];     // lanes whose search ended (cleared by the host)
-  long long t_start;
-  long long t_round;
-  unsigned long long pad[8];
-  MsRound rec[kRing];
-};
-
-struct MsParams {
-  int64_t n, nnz, words;
-  const int64_t *__restrict__ in_off;
-  const int32_t *__restrict__ in_idx;
-  const int64_t *__restrict__ out_off;
-  const int32_t *__restrict__ out_idx;
-  uint64_t *vis, *fr0, *fr1, *fr2;
-  uint32_t *touched0, *touched1;
-  int32_t *queue0, *queue1;
-  uint32_t *bigoff0, *bigoff1;
-  const int32_t *hub_slot;   // [n], -1 for non-hubs
-  const int32_t *hub_vtx;    // [nhub]
-  const int32_t *med_vtx;    // [nmed] vertices of in-degree in (kPullLight, kHubDeg]
-  int64_t nmed;
-  const uint32_t *hub_choff; // [nhub + 1] prefix of in-list chunks
-  uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
-  uint64_t *hub_found;       // [nhub][W] lanes found this round
-  int nhub;
-  int32_t *levels, *parents;  // batch mode: lane l at levels + l * n (start round 0)
-  const LaneTable *lanes;     // serving pool: per-lane outputs and start rounds
-  MsCtl *ctl;
-  cg_stats *stats;
-  int k;
-  int direction;
-  float ms_alpha;
-  int level_cap;
-  long long timeout_ns;
-  int resume;                 // continue from ctl->L instead of clearing and seeding
-  int max_rounds;             // stop after this many rounds in this launch
-  int stop_on_finish;         // stop after a round in which some lane's search ended
-  int finish_all;             // write -1 for every unreached (lane, vertex) at the end
-  int32_t roots[kMsMaxLanes];
-};
-
-template <int W>
-struct Mask {
-  uint64_t w[W];
-  __device__ __forceinline__ static Mask zero() {
-    Mask m;
-#pragma unroll
-    for (int i = 0; i < W; ++i) m.w[i] = 0;
-    return m;
-  }
-  __device__ __forceinline__ bool any() const {
-    uint64_t a = 0;
-#pragma unroll
-    for (int i = 0; i < W; ++i) a |= w[i];
-    return a != 0;
-  }
-  __device__ __forceinline__ int popc() const {
-    int c = 0;
-#pragma unroll
-    for (int i = 0; i < W; ++i) c += __popcll(w[i]);
-    return c;
-  }
-  __device__ __forceinline__ Mask operator&(const Mask &o) const {
-    Mask m;
-#pragma unroll
-    for (int i = 0; i < W; ++i) m.w[i] = w[i] & o.w[i];
-    return m;
-  }
-  __device__ __forceinline__ Mask operator|(const Mask &o) const {
-    Mask m;
-#pragma unroll
-    for (int i = 0; i < W; ++i) m.w[i] = w[i] | o.w[i];
-    return m;
-  }
-  __device__ __forceinline__ Mask andnot(const Mask &o) const {  // this & ~o
-    Mask m;
-#pragma unroll
-    for (int i = 0; i < W; ++i) m.w[i] = w[i] & ~o.w[i];
-    return m;
-  }
-  __device__ __forceinline__ bool operator==(const Mask &o) const {
-    bool e = true;
-#pragma unroll
-    for (int i = 0; i < W; ++i) e = e && (w[i] == o.w[i]);
-    return e;
-  }
-};
-
-template <int W>
-__device__ __forceinline__ Mask<W> ld_mask(const uint64_t *base, int64_t v) {
-  Mask<W> m;
-  if (W == 2) {
-    const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(base + v * 2);
-    m.w[0] = x.x;
-    m.w[W - 1] = x.y;
-  } else {
-#pragma unroll
-    for (int i = 0; i < W; ++i) m.w[i] = base[v * W + i];
-  }
-  return m;
-}
-
-template <int W>
-__device__ __forceinline__ void st_mask(uint64_t *base, int64_t v, const Mask<W> &m) {
-  if (W == 2) {
-    *reinterpret_cast<ulonglong2 *>(base + v * 2) = make_ulonglong2(m.w[0], m.w[W - 1]);
-  } else {
-#pragma unroll
-    for (int i = 0; i < W; ++i) base[v * W + i] = m.w[i];
-  }
-}
-
-template <int W>
-__device__ __forceinline__ Mask<W> lane_mask(int k) {
-  Mask<W> m;
-#pragma unroll
-  for (int i = 0; i < W; ++i) {
-    const int lo = i * 64;
-    m.w[i] = k >= lo + 64 ? ~0ull : (k <= lo ? 0ull : ((1ull << (k - lo)) - 1ull));
-  }
-  return m;
-}
-
-template <int W>
-__device__ __forceinline__ Mask<W> warp_or(Mask<W> m) {
-#pragma unroll
-  for (int j = 0; j < W; ++j)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m.w[j] |= __shfl_xor_sync(kMsFull, m.w[j], o);
-  return m;
-}
 
 // Output of lane l for vertex v discovered in round `round` (level round + 1
 // for a batch; relative to the lane's start round in a serving pool).
@@ -237,106 +67,55 @@ __device__ __forceinline__ void write_lanes(const MsParams &p, int64_t v, const 
   }
 }
 
-struct MsAcc {
-  unsigned long long nf = 0, visits = 0, mf = 0;
-  unsigned long long lanes[2] = {0ull, 0ull};
-};
-
-template <int W>
-__device__ __forceinline__ void acc_lanes(MsAcc &acc, const Mask<W> &m) {
-#pragma unroll
-  for (int i = 0; i < W; ++i) acc.lanes[i] |= m.w[i];
-}
-
-// Appends claimed vertices to a frontier list: light ones at the front of
-// `q`, big ones (out-degree > kLightMax) at the back with the prefix offset of
-// their edge lists (one packed atomic per warp: count << 32 | edges).  All 32
-// lanes call.
-__device__ __forceinline__ void ms_enqueue(bool claimed, int32_t v, int64_t deg, int32_t *q,
-                                           int64_t qcap, uint32_t *boff, unsigned *nlight,
-                                           unsigned long long *big, MsAcc &acc) {
-  const int lane = lane_id();
-  if (!__ballot_sync(kMsFull, claimed)) return;
-  const bool light = claimed && deg <= kLightMax;
-  const bool heavy = claimed && deg > kLightMax;
-  const unsigned below = (1u << lane) - 1u;
-  const unsigned ml = __ballot_sync(kMsFull, light);
-  if (ml) {
-    const int leader = __ffs(ml) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(nlight, (unsigned)__popc(ml));
-    base = __shfl_sync(kMsFull, base, leader);
-    if (light) q[base + __popc(ml & below)] = v;
-  }
-  const unsigned mb = __ballot_sync(kMsFull, heavy);
-  if (mb) {
-    const unsigned d = heavy ? (unsigned)deg : 0u;
-    unsigned incl = d;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(kMsFull, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const unsigned total = __shfl_sync(kMsFull, incl, 31);
-    unsigned long long old = 0;
-    if (lane == 0) old = atomicAdd(big, ((unsigned long long)__popc(mb) << 32) | total);
-    old = __shfl_sync(kMsFull, old, 0);
-    if (heavy) {
-      const unsigned idx = (unsigned)(old >> 32) + __popc(mb & below);
-      q[qcap - 1 - (int64_t)idx] = v;
-      boff[idx] = (unsigned)(old & 0xffffffffu) + incl - d;
-    }
-  }
-  if (claimed) {
-    acc.nf += 1;
-    acc.mf += (unsigned long long)deg;
-  }
-}
-
-__device__ __forceinline__ unsigned long long ms_warp_sum(unsigned long long x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(kMsFull, x, o);
-  return x;
-}
-
 // Warp-cooperative scan of in-list entries [s, e) of vertex v (all lanes call
-// with the same arguments): 32 sources per step; for each lane bit found in a
-// step, the lowest warp lane holding it -- the smallest source -- wins.  Stops
-// once every wanted bit is found.  With hub >= 0 the winners go to the hub's
-// candidate buffer by atomicMin; otherwise they are written as outputs.
+// with the same arguments): 4 x 32 sources per step, their index and mask
+// loads in flight together, taken 32 at a time in ascending order; for each
+// lane bit found among 32 sources the lowest warp lane holding it -- the
+// smallest source -- wins.  Stops once every wanted bit is found.  With
+// hub >= 0 the winners go to the hub's candidate buffer by atomicMin;
+// otherwise they are written as outputs.
 template <int W>
 __device__ Mask<W> warp_scan(const MsParams &p, int64_t v, int64_t s, int64_t e,
                              const Mask<W> &want, const uint64_t *cur, int level, int hub) {
+  constexpr int G = 4;
   const int lane = lane_id();
   Mask<W> got = Mask<W>::zero();
-  for (int64_t base = s; base < e; base += 32) {
-    const int64_t i = base + lane;
-    Mask<W> f = Mask<W>::zero();
-    int32_t u = 0;
-    if (i < e) {
-      u = __ldg(p.in_idx + i);
-      f = (ld_mask<W>(cur, u) & want).andnot(got);
-    }
-    const Mask<W> F = warp_or<W>(f);
-    if (F.any()) {
+  for (int64_t base = s; base < e; base += 32 * G) {
+    int32_t u[G];
+    Mask<W> f[G];
 #pragma unroll
-      for (int j = 0; j < W; ++j) {
-        uint64_t bits = F.w[j];
-        while (bits) {
-          const int b = __ffsll((long long)bits) - 1;
-          bits &= bits - 1;
-          const unsigned who = __ballot_sync(kMsFull, (f.w[j] >> b) & 1ull);
-          if (lane == __ffs(who) - 1) {
-            if (hub >= 0)
-              atomicMin(p.hub_cand + (int64_t)hub * (64 * W) + j * 64 + b, (unsigned)u);
-            else
-              write_lane(p, j * 64 + b, v, u, level);
+    for (int k = 0; k < G; ++k) {
+      const int64_t i = base + 32 * k + lane;
+      u[k] = i < e ? __ldg(p.in_idx + i) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < G; ++k) f[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+    bool done = false;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      if (!done) {
+        const Mask<W> fk = (f[k] & want).andnot(got);
+        const Mask<W> F = warp_or<W>(fk);
+        if (F.any()) {
+          const Mask<W> mine = first_holder<W>(fk);
+#pragma unroll
+          for (int j = 0; j < W; ++j) {
+            uint64_t bits = mine.w[j];
+            while (bits) {
+              const int b = __ffsll((long long)bits) - 1;
+              bits &= bits - 1;
+              if (hub >= 0)
+                atomicMin(p.hub_cand + (int64_t)hub * (64 * W) + j * 64 + b, (unsigned)u[k]);
+              else
+                write_lane(p, j * 64 + b, v, u[k], level);
+            }
           }
+          got = got | F;
+          done = got == want;
         }
       }
-      got = got | F;
-      if (got == want) break;
     }
+    if (done) break;
   }
   return got;
 }
@@ -534,187 +313,6 @@ __device__ void ms_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   if (p.nhub > 0) hub_chunks<W>(p, cur, active, L);
 }
 
-// Edge u -> v of a push round.  Hub targets take parent candidates directly;
-// other targets get their lanes ORed into the next mask, and the one thread
-// that first touches v this round queues it.
-template <int W>
-__device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, int32_t u,
-                                         int32_t v, uint64_t *nxt, uint32_t *touched) {
-  const Mask<W> f = fu.andnot(ld_mask<W>(p.vis, v));
-  if (!f.any()) return false;
-  const int h = p.hub_slot[v];
-  if (h >= 0) {
-    const Mask<W> have = ld_mask<W>(p.hub_found, h);
-#pragma unroll
-    for (int j = 0; j < W; ++j) {
-      uint64_t bits = f.w[j];
-      while (bits) {
-        const int b = __ffsll((long long)bits) - 1;
-        bits &= bits - 1;
-        atomicMin(p.hub_cand + (int64_t)h * (64 * W) + j * 64 + b, (unsigned)u);
-      }
-      const uint64_t add = f.w[j] & ~have.w[j];
-      if (add)
-        atomicOr(reinterpret_cast<unsigned long long *>(p.hub_found + (int64_t)h * W + j),
-                 (unsigned long long)add);
-    }
-    return false;
-  }
-  const Mask<W> add = f.andnot(ld_mask<W>(nxt, v));
-  if (add.any()) {
-#pragma unroll
-    for (int i = 0; i < W; ++i)
-      if (add.w[i])
-        atomicOr(reinterpret_cast<unsigned long long *>(nxt + (int64_t)v * W + i),
-                 (unsigned long long)add.w[i]);
-  }
-  const uint32_t tb = 1u << (v & 31);
-  if (touched[v >> 5] & tb) return false;
-  return (atomicOr(touched + (v >> 5), tb) & tb) == 0;
-}
-
-template <int W>
-__device__ __forceinline__ void ms_push_step(const MsParams &p, bool valid, const Mask<W> &fu,
-                                             int32_t u, int64_t e, uint64_t *nxt,
-                                             uint32_t *touched, int32_t *q, uint32_t *boff,
-                                             MsRound *Rn, MsAcc &acc) {
-  bool claimed = false;
-  int32_t v = 0;
-  int64_t deg = 0;
-  if (valid) {
-    v = __ldg(p.out_idx + e);
-    claimed = ms_relax<W>(p, fu, u, v, nxt, touched);
-    if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
-  }
-  ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
-}
-
-// Walks edge positions [x0, x1) of a big-vertex list (vertices q[cap-1-j],
-// prefix offsets boff[j], all of out-degree > 32).
-template <int W>
-__device__ void ms_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *nxt,
-                              uint32_t *touched, const int32_t *bq, int64_t cap,
-                              const uint32_t *boff, unsigned nbig, unsigned x0, unsigned x1,
-                              int32_t *q, uint32_t *qoff, MsRound *Rn, MsAcc &acc) {
-  const int lane = lane_id();
-  unsigned lo = 0, hi = nbig - 1;
-  while (lo < hi) {
-    const unsigned mid = (lo + hi + 1) >> 1;
-    if (boff[mid] <= x0)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  unsigned j = lo;
-  int32_t vj = bq[cap - 1 - (int64_t)j];
-  int64_t sj = __ldg(p.out_off + vj);
-  unsigned oj = boff[j];
-  unsigned endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
-  Mask<W> fj = ld_mask<W>(cur, vj);
-  for (unsigned base = x0; base < x1; base += 32) {
-    while (base >= endj) {
-      ++j;
-      vj = bq[cap - 1 - (int64_t)j];
-      sj = __ldg(p.out_off + vj);
-      oj = boff[j];
-      endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
-      fj = ld_mask<W>(cur, vj);
-    }
-    const unsigned x = base + lane;
-    const bool valid = x < x1;
-    int32_t u = vj;
-    int64_t e = sj + (int64_t)(x - oj);
-    Mask<W> fu = fj;
-    if (__ballot_sync(kMsFull, valid && x >= endj)) {
-      const int32_t vn = bq[cap - 1 - (int64_t)(j + 1)];
-      if (valid && x >= endj) {
-        u = vn;
-        e = __ldg(p.out_off + vn) + (int64_t)(x - endj);
-        fu = ld_mask<W>(cur, vn);
-      }
-    }
-    ms_push_step<W>(p, valid, fu, u, e, nxt, touched, q, qoff, Rn, acc);
-  }
-}
-
-template <int W>
-__device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
-                        uint32_t *touched, MsRound *Rc, MsRound *Rn, MsAcc &acc) {
-  __shared__ int32_t s_u[kMsBlock / 32][32];
-  __shared__ int64_t s_s[kMsBlock / 32][32];
-  __shared__ int64_t s_x[kMsBlock / 32][32];
-  const int lane = lane_id();
-  const int wib = threadIdx.x >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int parity = L & 1, next_parity = parity ^ 1;
-  const int32_t *qc = parity ? p.queue1 : p.queue0;
-  const uint32_t *bc = parity ? p.bigoff1 : p.bigoff0;
-  int32_t *qn = next_parity ? p.queue1 : p.queue0;
-  uint32_t *bn = next_parity ? p.bigoff1 : p.bigoff0;
-
-  const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
-  const unsigned nbig = (unsigned)(bigw >> 32), big_edges = (unsigned)bigw;
-  const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
-  // chunks of 32 .. kPushChunk edges: small frontiers still spread over the grid
-  unsigned chunk = ((big_edges / (unsigned)nwarps) + 31u) & ~31u;
-  chunk = chunk < 32u ? 32u : (chunk > (unsigned)kPushChunk ? (unsigned)kPushChunk : chunk);
-  const unsigned nb = (big_edges + chunk - 1) / chunk;
-  const unsigned nitems = nb + (nlight + 31u) / 32u;
-  unsigned item = (unsigned)warp_id_global();
-  while (item < nitems) {
-    if (item < nb) {
-      const unsigned x0 = item * chunk;
-      ms_push_chunk<W>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0, min(x0 + chunk, big_edges),
-                       qn, bn, Rn, acc);
-    } else {
-      const unsigned idx = (item - nb) * 32u + lane;
-      int32_t u = -1;
-      int64_t s = 0, d = 0;
-      if (idx < nlight) {
-        u = qc[idx];
-        s = __ldg(p.out_off + u);
-        d = __ldg(p.out_off + u + 1) - s;
-      }
-      int64_t incl = d;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int64_t t = __shfl_up_sync(kMsFull, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const int64_t total = __shfl_sync(kMsFull, incl, 31);
-      s_u[wib][lane] = u;
-      s_s[wib][lane] = s;
-      s_x[wib][lane] = incl - d;
-      __syncwarp();
-      for (int64_t base = 0; base < total; base += 32) {
-        const int64_t t = base + lane;
-        const bool valid = t < total;
-        int64_t e = 0;
-        int32_t uu = 0;
-        Mask<W> fu = Mask<W>::zero();
-        if (valid) {
-          int lo = 0, hi = 31;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_x[wib][mid] <= t)
-              lo = mid;
-            else
-              hi = mid - 1;
-          }
-          uu = s_u[wib][lo];
-          fu = ld_mask<W>(cur, uu);
-          e = s_s[wib][lo] + (t - s_x[wib][lo]);
-        }
-        ms_push_step<W>(p, valid, fu, uu, e, nxt, touched, qn, bn, Rn, acc);
-      }
-      __syncwarp();
-    }
-    unsigned nextitem = 0;
-    if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
-    item = __shfl_sync(kMsFull, nextitem, 0);
-  }
-}
-
 // After a push round: every newly reached non-hub vertex merges its lanes
 // into vis and finds each lane's parent by scanning its ascending in-list
 // (it ends: every lane has a frontier source there).  Hubs are finalized from
@@ -748,42 +346,6 @@ __device__ void ms_resolve(const MsParams &p, int L, const uint64_t *cur, uint64
   }
   if (p.nhub > 0) hub_finalize<W>(p, L, nxt, Rn, acc);
 }
-
-// Block totals of the per-thread counters (thread 0 gets them) -- the one
-// __syncthreads of a round's end before the grid-wide wait.
-__device__ void ms_block_totals(MsAcc &acc, MsAcc &tot) {
-  __shared__ unsigned long long s_red[5][kMsBlock / 32];
-  const int lane = lane_id(), wib = threadIdx.x >> 5;
-  const unsigned long long a = ms_warp_sum(acc.nf), b = ms_warp_sum(acc.visits),
-                           c = ms_warp_sum(acc.mf);
-  unsigned long long l0 = acc.lanes[0], l1 = acc.lanes[1];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    l0 |= __shfl_xor_sync(kMsFull, l0, o);
-    l1 |= __shfl_xor_sync(kMsFull, l1, o);
-  }
-  if (lane == 0) {
-    s_red[0][wib] = a;
-    s_red[1][wib] = b;
-    s_red[2][wib] = c;
-    s_red[3][wib] = l0;
-    s_red[4][wib] = l1;
-  }
-  __syncthreads();
-  tot = MsAcc();
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-      tot.nf += s_red[0][i];
-      tot.visits += s_red[1][i];
-      tot.mf += s_red[2][i];
-      tot.lanes[0] |= s_red[3][i];
-      tot.lanes[1] |= s_red[4][i];
-    }
-  }
-  acc = MsAcc();
-}
-
-constexpr unsigned kMsStop = 1u, kMsNextPull = 2u;
 
 // End of round L, run by the block that arrives last: termination (no lane
 // has a frontier), lanes whose search ended this round, the direction of the
@@ -881,6 +443,7 @@ struct MsSetupDecision {
     ctl->t_round = now;
     ctl->pull_rounds = 0;
     ctl->switches = 0;
+    ctl->exited = 0u;
     return 0u;
   }
 };
@@ -892,6 +455,7 @@ struct MsSetupDecision {
 template <int W>
 __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
   __shared__ unsigned s_payload;
+  if (p.gate && *(volatile int *)p.flag == 0) return;  // the ledger pass succeeded
   MsCtl *ctl = p.ctl;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
@@ -982,7 +546,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
         hub_finalize<W>(p, L, nxt, Rn, acc);
       }
     } else {
-      ms_push<W>(p, L, cur, nxt, touched, Rc, Rn, acc);
+      ms_push<W, false>(p, L, cur, nxt, touched, Rc, Rn, acc);
       __syncthreads();
       if (threadIdx.x == 0)
         s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
@@ -1030,6 +594,12 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
     }
   }
   if (leader && !ok) p.stats->status = *(volatile int *)&ctl->status;
+  // the last block out records the time from the end of the last round
+  if (ok) {
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(&ctl->exited, 1u) + 1u == gridDim.x)
+      p.stats->finish_ns = global_ns() - *(volatile long long *)&ctl->t_round;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1060,24 +630,6 @@ __global__ void hub_chunks_kernel(int nhub, const int64_t *__restrict__ in_off,
   }
 }
 
-struct MsState {
-  uint64_t *bits = nullptr;
-  uint32_t *touched = nullptr;
-  int32_t *queue = nullptr;
-  uint32_t *bigoff = nullptr;
-  int32_t *hub_slot = nullptr;
-  int32_t *hub_vtx = nullptr;
-  int32_t *med_vtx = nullptr;
-  int64_t nmed = 0;
-  uint32_t *hub_choff = nullptr;
-  uint32_t *hub_cand = nullptr;
-  uint64_t *hub_found = nullptr;
-  MsCtl *ctl = nullptr;
-  int64_t bcap = 0;
-  int nhub = 0;
-  int lane_words = 0;
-};
-
 static void ms_free_state(MsState *s) {
   if (!s) return;
   cudaFree(s->bits);
@@ -1091,6 +643,11 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->hub_cand);
   cudaFree(s->hub_found);
   cudaFree(s->ctl);
+  cudaFree(s->flag);
+  cudaFree(s->cand_slot);
+  cudaFree(s->cand_vtx);
+  cudaFree(s->cand_choff);
+  cudaFree(s->cand);
   delete s;
 }
 
@@ -1169,22 +726,79 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
   return rc;
 }
 
+__global__ void slot_map_kernel(int count, const int32_t *__restrict__ vtx, int32_t *slot) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    slot[vtx[i]] = i;
+}
+
+// Parent-candidate slots of the output pass of a ledger batch: every vertex of
+// in-degree > kPullLight (the medium list, then the hubs) gets a slot of 64 W
+// candidates and its in-list is cut into kHubChunk-entry chunks.
+static int ms_build_cands(cg_graph *g, MsState *s) {
+  const int64_t ncand = s->nmed + s->nhub;
+  s->ncand = (int)ncand;
+  const size_t nc = ncand > 0 ? (size_t)ncand : 1;
+  if (cudaMalloc(&s->cand_slot, sizeof(int32_t) * (size_t)g->n) != cudaSuccess ||
+      cudaMalloc(&s->cand_vtx, sizeof(int32_t) * nc) != cudaSuccess ||
+      cudaMalloc(&s->cand_choff, sizeof(uint32_t) * (nc + 1)) != cudaSuccess ||
+      cudaMalloc(&s->cand, sizeof(uint32_t) * nc * 64 * s->lane_words) != cudaSuccess)
+    return CG_ERR_OUT_OF_MEMORY;
+  CG_CUDA(cudaMemsetAsync(s->cand_slot, 0xff, sizeof(int32_t) * (size_t)g->n, g->stream));
+  if (s->nmed)
+    CG_CUDA(cudaMemcpyAsync(s->cand_vtx, s->med_vtx, sizeof(int32_t) * (size_t)s->nmed,
+                            cudaMemcpyDeviceToDevice, g->stream));
+  if (s->nhub)
+    CG_CUDA(cudaMemcpyAsync(s->cand_vtx + s->nmed, s->hub_vtx, sizeof(int32_t) * (size_t)s->nhub,
+                            cudaMemcpyDeviceToDevice, g->stream));
+  uint32_t *chunks = nullptr;
+  CG_CUDA(cudaMalloc(&chunks, sizeof(uint32_t) * nc));
+  int rc = CG_OK;
+  uint32_t *h = new (std::nothrow) uint32_t[nc + 1];
+  do {
+    if (!h) { rc = CG_ERR_OUT_OF_MEMORY; break; }
+    h[0] = 0;
+    if (ncand > 0) {
+      const int blocks = (int)((ncand + 255) / 256 < g->num_sms * 16 ? (ncand + 255) / 256
+                                                                      : g->num_sms * 16);
+      slot_map_kernel<<<blocks, 256, 0, g->stream>>>((int)ncand, s->cand_vtx, s->cand_slot);
+      hub_chunks_kernel<<<blocks, 256, 0, g->stream>>>((int)ncand, g->in_off, s->cand_vtx, chunks);
+      cudaError_t e = cudaMemcpyAsync(h + 1, chunks, sizeof(uint32_t) * (size_t)ncand,
+                                      cudaMemcpyDeviceToHost, g->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "candidate chunks"); break; }
+      for (int64_t i = 0; i < ncand; ++i) h[i + 1] += h[i];
+    }
+    cudaError_t e = cudaMemcpyAsync(s->cand_choff, h, sizeof(uint32_t) * (size_t)(ncand + 1),
+                                    cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "candidate chunks"); break; }
+    g->device_bytes += sizeof(int32_t) * (g->n + nc) + sizeof(uint32_t) * (nc + 1) +
+                       sizeof(uint32_t) * nc * 64 * s->lane_words;
+  } while (0);
+  delete[] h;
+  cudaFree(chunks);
+  return rc;
+}
+
 // Lane state for one batched search stream (a graph's batch state or a pool).
-static int ms_create_state(cg_graph *g, int lane_words, MsState **out) {
+static int ms_create_state(cg_graph *g, int lane_words, int hist_planes, MsState **out) {
   MsState *s = new MsState();
   s->lane_words = lane_words;
   s->bcap = bfs_big_capacity(g->n, g->nnz);
-  const size_t bits = sizeof(uint64_t) * 4 * (size_t)g->n * lane_words;
+  s->hist_planes = hist_planes > 3 ? hist_planes : 3;
+  const size_t bits = sizeof(uint64_t) * (1 + (size_t)s->hist_planes) * (size_t)g->n * lane_words;
   const size_t words = (size_t)((g->n + 31) / 32);
   if (cudaMalloc(&s->bits, bits) != cudaSuccess ||
       cudaMalloc(&s->touched, sizeof(uint32_t) * 2 * words) != cudaSuccess ||
       cudaMalloc(&s->queue, sizeof(int32_t) * 2 * (size_t)g->n) != cudaSuccess ||
       cudaMalloc(&s->bigoff, sizeof(uint32_t) * 2 * (size_t)s->bcap) != cudaSuccess ||
-      cudaMalloc(&s->ctl, sizeof(MsCtl)) != cudaSuccess) {
+      cudaMalloc(&s->ctl, sizeof(MsCtl)) != cudaSuccess ||
+      cudaMalloc(&s->flag, sizeof(int)) != cudaSuccess) {
     ms_free_state(s);
     return CG_ERR_OUT_OF_MEMORY;
   }
   int rc = ms_build_hubs(g, s);
+  if (!rc && s->hist_planes >= 4) rc = ms_build_cands(g, s);
   if (rc) {
     ms_free_state(s);
     return rc;
@@ -1195,13 +809,36 @@ static int ms_create_state(cg_graph *g, int lane_words, MsState **out) {
   return CG_OK;
 }
 
+// Frontier planes of a graph's batch state: the round history F_0 .. F_D of
+// the ledger kernel when the option allows it and memory holds at least four
+// planes (D = 64 at most, within a quarter of free memory and 16 GiB), else
+// the three rotating planes of the direct kernel.
+static int ms_history_planes(const cg_graph *g, int lane_words) {
+  const int want = g->opt.ms_history;
+  if (want < 0) return 3;
+  const size_t plane = sizeof(uint64_t) * (size_t)g->n * (size_t)lane_words;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 3;
+  size_t budget = free_b / 4;
+  const size_t cap = (size_t)16 << 30;
+  if (budget > cap) budget = cap;
+  long long planes = (long long)(budget / plane);
+  // at most CG_HISTORY + 1 planes: the output pass reads each level's round
+  // direction from the statistics' history
+  const long long most = want > 0 && want < CG_HISTORY ? (long long)want + 1 : CG_HISTORY + 1;
+  if (planes > most) planes = most;
+  return planes >= 4 ? (int)planes : 3;
+}
+
 static int ms_alloc_state(cg_graph *g, int lane_words) {
-  if (g->ms_ctl && g->ms_lane_words == lane_words) return CG_OK;
-  ms_free_state(reinterpret_cast<MsState *>(g->ms_ctl));
+  MsState *old = reinterpret_cast<MsState *>(g->ms_ctl);
+  if (old && g->ms_lane_words == lane_words && old->hist_opt == g->opt.ms_history) return CG_OK;
+  ms_free_state(old);
   g->ms_ctl = nullptr;
   MsState *s = nullptr;
-  int rc = ms_create_state(g, lane_words, &s);
+  int rc = ms_create_state(g, lane_words, ms_history_planes(g, lane_words), &s);
   if (rc) return rc;
+  s->hist_opt = g->opt.ms_history;
   g->ms_ctl = s;
   g->ms_lane_words = lane_words;
   return CG_OK;
@@ -1225,55 +862,6 @@ int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems) {
     g->ms_out_cap = out_elems;
   }
   return CG_OK;
-}
-
-// Fields of a launch shared by batches and serving pools.
-template <int W>
-static MsParams ms_params(const cg_graph *g, const MsState *s) {
-  MsParams p;
-  p.n = g->n;
-  p.nnz = g->nnz;
-  p.words = (g->n + 31) / 32;
-  p.in_off = g->in_off;
-  p.in_idx = g->in_idx;
-  p.out_off = g->out_off;
-  p.out_idx = g->out_idx;
-  const size_t plane = (size_t)g->n * W;
-  p.vis = s->bits;
-  p.fr0 = s->bits + plane;
-  p.fr1 = s->bits + 2 * plane;
-  p.fr2 = s->bits + 3 * plane;
-  p.touched0 = s->touched;
-  p.touched1 = s->touched + p.words;
-  p.queue0 = s->queue;
-  p.queue1 = s->queue + g->n;
-  p.bigoff0 = s->bigoff;
-  p.bigoff1 = s->bigoff + s->bcap;
-  const int64_t nh = s->nhub > 0 ? s->nhub : 1;
-  p.hub_slot = s->hub_slot;
-  p.hub_vtx = s->hub_vtx;
-  p.med_vtx = s->med_vtx;
-  p.nmed = s->nmed;
-  p.hub_choff = s->hub_choff;
-  p.hub_cand = s->hub_cand;
-  p.hub_found = s->hub_found;
-  p.nhub = s->nhub;
-  p.levels = p.parents = nullptr;
-  p.lanes = nullptr;
-  p.ctl = s->ctl;
-  p.stats = g->d_stats;
-  p.k = 0;
-  p.resume = 0;
-  p.max_rounds = 0x7fffffff;
-  p.stop_on_finish = 0;
-  p.finish_all = 0;
-  p.direction = g->opt.direction == CG_DIR_TAU ? CG_DIR_AUTO : g->opt.direction;
-  p.ms_alpha = g->opt.ms_alpha > 0 ? g->opt.ms_alpha : 4.f;
-  p.level_cap = g->opt.level_cap > 0 ? g->opt.level_cap
-                                     : (int)((g->n + 1) < 0x7fffffff ? g->n + 1 : 0x7fffffff);
-  p.timeout_ns = (long long)(g->opt.wait_timeout_ms > 0 ? g->opt.wait_timeout_ms : 1000) * 1000000ll;
-  for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = 0;
-  return p;
 }
 
 template <int W>
@@ -1300,16 +888,6 @@ static int ms_launch(const cg_graph *g, const MsParams &p, cudaStream_t stream) 
   return CG_OK;
 }
 
-// Clean control block and hub candidates for a fresh launch on `s`.
-template <int W>
-static int ms_reset(const MsState *s, cudaStream_t stream) {
-  const int64_t nh = s->nhub > 0 ? s->nhub : 1;
-  CG_CUDA(cudaMemsetAsync(s->ctl, 0, sizeof(MsCtl), stream));
-  CG_CUDA(cudaMemsetAsync(s->hub_cand, 0xff, sizeof(uint32_t) * (size_t)nh * 64 * W, stream));
-  CG_CUDA(cudaMemsetAsync(s->hub_found, 0, sizeof(uint64_t) * (size_t)nh * W, stream));
-  return CG_OK;
-}
-
 template <int W>
 static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
                           int32_t *d_levels, int32_t *d_parents) {
@@ -1324,6 +902,22 @@ static int ms_launch_pass(cg_graph *g, MsState *s, const int64_t *roots, int k,
   return ms_launch<W>(g, p, g->stream);
 }
 
+// The direct kernel as the fallback of a ledger pass: it returns at once
+// unless the ledger kernel set the overflow flag (the output pass has then
+// cleared the control block).
+template <int W>
+static int ms_launch_gated(cg_graph *g, MsState *s, const int64_t *roots, int k,
+                           int32_t *d_levels, int32_t *d_parents) {
+  MsParams p = ms_params<W>(g, s);
+  p.levels = d_levels;
+  p.parents = d_parents;
+  p.k = k;
+  p.finish_all = 1;
+  p.gate = 1;
+  for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = i < k ? (int32_t)roots[i] : 0;
+  return ms_launch<W>(g, p, g->stream);
+}
+
 int msbfs_launch(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels,
                  int32_t *d_parents) {
   const int W = g->opt.lane_words == 2 ? 2 : 1;
@@ -1335,8 +929,16 @@ int msbfs_launch(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels
     const int kk = (k - b) < lanes ? (k - b) : lanes;
     int32_t *lv = d_levels + (int64_t)b * g->n;
     int32_t *pa = d_parents + (int64_t)b * g->n;
-    rc = W == 2 ? ms_launch_pass<2>(g, s, roots + b, kk, lv, pa)
-                : ms_launch_pass<1>(g, s, roots + b, kk, lv, pa);
+    if (s->hist_planes >= 4) {
+      // rounds on masks + one output pass; the direct kernel runs only if the
+      // search outgrew the history
+      rc = ms_ledger_pass(g, s, roots + b, kk, lv, pa);
+      if (!rc) rc = W == 2 ? ms_launch_gated<2>(g, s, roots + b, kk, lv, pa)
+                           : ms_launch_gated<1>(g, s, roots + b, kk, lv, pa);
+    } else {
+      rc = W == 2 ? ms_launch_pass<2>(g, s, roots + b, kk, lv, pa)
+                  : ms_launch_pass<1>(g, s, roots + b, kk, lv, pa);
+    }
     if (rc) return rc;
   }
   return CG_OK;
@@ -1494,7 +1096,7 @@ int cg_pool_create(cg_graph *g, int32_t lane_words, cg_pool **out) {
   if (!pl) return CG_ERR_OUT_OF_MEMORY;
   pl->g = g;
   pl->W = lane_words;
-  int rc = ms_create_state(g, lane_words, &pl->s);
+  int rc = ms_create_state(g, lane_words, 0, &pl->s);
   if (!rc && (cudaMalloc(&pl->d_lanes, sizeof(LaneTable)) != cudaSuccess ||
               cudaMalloc(&pl->d_out, sizeof(unsigned long long) * 4) != cudaSuccess ||
               cudaHostAlloc(&pl->h_out, sizeof(unsigned long long) * 4, cudaHostAllocDefault) !=

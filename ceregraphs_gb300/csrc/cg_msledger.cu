@@ -1,0 +1,848 @@
+// Multi-source BFS with the outputs written after the search ("ledger"
+// mode).  The rounds advance only the W-word lane masks: vis, and the
+// frontier F_L of every round, kept as a history F_0 .. F_D in HBM.  Nothing
+// is written per (lane, vertex) while the rounds run.  One output pass after
+// the last round then writes every (lane, vertex) output exactly once:
+//   level(l, v)  = the round L whose F_L[v] holds bit l      (-1 if none)
+//   parent(l, v) = roots[l] if level 1, else the lowest in-neighbour u of v
+//                  with bit l in F_{level - 1}[u]
+// which is the lowest-index rule of the per-root search and of the direct
+// batched kernel (bfs/README.md:208-224), so the outputs are identical.
+//
+// Why: written during the rounds, every discovery is a 4-byte store into one
+// of 64 rows -- 32 scattered stores per warp instruction, each a separate L1
+// wavefront and L2 transaction, and sectors completed across rounds (partial
+// sector writes).  Here the output pass stages a 32-vertex x 64-lane tile per
+// warp in shared memory and writes each lane's 32 values as one 128-byte row.
+//
+// Rounds: a pull round ORs the frontier masks of a vertex's in-neighbours
+// until every wanted lane is found (no order needed: parents come later); a
+// push round ORs frontier masks into out-neighbours' next masks with
+// atomicOr, then merges them into vis.  Hubs' in-lists are split into chunks
+// across warps as in the direct kernel.
+//
+// A search that needs more rounds than the history holds sets a flag and
+// stops; the output pass then only clears the control block, and the direct
+// kernel, launched after it gated on the flag, runs the batch from scratch.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_ms.cuh"
+
+namespace cg {
+namespace {
+
+constexpr int kOutBlock = 256;                 // output pass: 8 warps a block
+constexpr int kOutWarps = kOutBlock / 32;
+constexpr int kOutLevels = 4;                  // levels resolved per in-list scan
+constexpr int kParStride = 65;                 // shared row strides (bank-conflict free)
+constexpr int kLvlStride = 68;
+constexpr int kOutWarpBytes = 32 * kParStride * 4 + 32 * kLvlStride;
+
+template <int W>
+__device__ __forceinline__ uint64_t *plane(const MsParams &p, int L) {
+  return p.hist + (int64_t)L * p.n * W;
+}
+
+// OR of the frontier masks of in-list entries [s, e) restricted to `want`,
+// one thread, four entries' loads in flight; stops once all of want is found.
+template <int W>
+__device__ __forceinline__ Mask<W> or_thread(const MsParams &p, int64_t s, int64_t e,
+                                             const Mask<W> &want, const uint64_t *cur) {
+  constexpr int G = 4;
+  Mask<W> got = Mask<W>::zero();
+  for (int64_t i0 = s; i0 < e; i0 += G) {
+    int32_t u[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) u[k] = i0 + k < e ? __ldg(p.in_idx + i0 + k) : -1;
+#pragma unroll
+    for (int k = 0; k < G; ++k)
+      if (u[k] >= 0) got = got | (ld_mask<W>(cur, u[k]) & want);
+    if (got == want) break;
+  }
+  return got;
+}
+
+// The same by a whole warp (all lanes call with the same arguments), 4 x 32
+// entries per step.
+template <int W>
+__device__ __forceinline__ Mask<W> or_warp(const MsParams &p, int64_t s, int64_t e,
+                                           const Mask<W> &want, const uint64_t *cur) {
+  constexpr int G = 4;
+  const int lane = lane_id();
+  Mask<W> got = Mask<W>::zero();
+  for (int64_t base = s; base < e; base += 32 * G) {
+    int32_t u[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const int64_t i = base + 32 * k + lane;
+      u[k] = i < e ? __ldg(p.in_idx + i) : -1;
+    }
+    Mask<W> f = Mask<W>::zero();
+#pragma unroll
+    for (int k = 0; k < G; ++k)
+      if (u[k] >= 0) f = f | ld_mask<W>(cur, u[k]);
+    got = got | warp_or<W>(f & want);
+    if (got == want) break;
+  }
+  return got;
+}
+
+// Pull round: light vertices one thread each, medium vertices one warp each,
+// hub in-lists by chunks (ORed into hub_found, merged after the wait).
+template <int W>
+__device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
+                        const Mask<W> &active, MsRound *Rn, MsAcc &acc) {
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int next_parity = (L + 1) & 1;
+  int32_t *q = next_parity ? p.queue1 : p.queue0;
+  uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+       base < p.n; base += nthreads) {
+    const int64_t v = base + lane_id();
+    Mask<W> want = Mask<W>::zero();
+    Mask<W> seen = Mask<W>::zero();
+    int64_t s = 0, e = 0;
+    if (v < p.n) {
+      seen = ld_mask<W>(p.vis, v);
+      want = active.andnot(seen);
+      if (want.any()) {
+        s = __ldg(p.in_off + v);
+        e = __ldg(p.in_off + v + 1);
+        if (e - s > kPullLight) want = Mask<W>::zero();  // medium list or hub chunks
+      }
+    }
+    if (!__ballot_sync(kMsFull, want.any())) continue;
+    Mask<W> got = Mask<W>::zero();
+    if (want.any()) got = or_thread<W>(p, s, e, want, cur);
+    bool claimed = false;
+    int64_t deg = 0;
+    if (got.any()) {
+      st_mask<W>(nxt, v, got);
+      st_mask<W>(p.vis, v, seen | got);
+      claimed = true;
+      acc.visits += (unsigned long long)got.popc();
+      acc_lanes<W>(acc, got);
+      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+    }
+    ms_enqueue(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+  }
+  const int nwarps = (int)(nthreads >> 5);
+  for (int64_t j = warp_id_global(); j < p.nmed; j += nwarps) {
+    const int32_t v = p.med_vtx[j];
+    const Mask<W> seen = ld_mask<W>(p.vis, v);
+    const Mask<W> want = active.andnot(seen);
+    if (!want.any()) continue;
+    const Mask<W> got = or_warp<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1), want, cur);
+    const bool claimed = lane_id() == 0 && got.any();
+    int64_t deg = 0;
+    if (claimed) {
+      st_mask<W>(nxt, v, got);
+      st_mask<W>(p.vis, v, seen | got);
+      acc.visits += (unsigned long long)got.popc();
+      acc_lanes<W>(acc, got);
+      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+    }
+    ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+  }
+  if (p.nhub == 0) return;
+  const unsigned nchunks = p.hub_choff[p.nhub];
+  for (unsigned c = (unsigned)warp_id_global(); c < nchunks; c += (unsigned)nwarps) {
+    unsigned lo = 0, hi = (unsigned)p.nhub - 1;
+    while (lo < hi) {
+      const unsigned mid = (lo + hi + 1) >> 1;
+      if (p.hub_choff[mid] <= c)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int h = (int)lo;
+    const int32_t v = p.hub_vtx[h];
+    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v));
+    if (!want.any()) continue;
+    const int64_t s = __ldg(p.in_off + v) + (int64_t)(c - p.hub_choff[h]) * kHubChunk;
+    const int64_t e = min(s + (int64_t)kHubChunk, __ldg(p.in_off + v + 1));
+    const Mask<W> got = or_warp<W>(p, s, e, want, cur);
+    if (lane_id() == 0) {
+#pragma unroll
+      for (int j = 0; j < W; ++j)
+        if (got.w[j])
+          atomicOr(reinterpret_cast<unsigned long long *>(p.hub_found + (int64_t)h * W + j),
+                   (unsigned long long)got.w[j]);
+    }
+  }
+}
+
+// After the wait that ends a pull round's scans: hubs found this round get
+// their next mask and vis, and are queued after the round's other vertices.
+template <int W>
+__device__ void lg_hub_merge(const MsParams &p, int L, uint64_t *nxt, MsRound *Rn, MsAcc &acc) {
+  const int lane = lane_id();
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int next_parity = (L + 1) & 1;
+  int32_t *q = next_parity ? p.queue1 : p.queue0;
+  uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
+  for (int64_t h0 = (int64_t)warp_id_global() * 32; h0 < p.nhub; h0 += (int64_t)nwarps * 32) {
+    const int64_t h = h0 + lane;
+    bool claimed = false;
+    int32_t v = 0;
+    int64_t deg = 0;
+    if (h < p.nhub) {
+      const Mask<W> found = ld_mask<W>(p.hub_found, h);
+      if (found.any()) {
+        v = p.hub_vtx[h];
+        st_mask<W>(nxt, v, found);
+        st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | found);
+        st_mask<W>(p.hub_found, h, Mask<W>::zero());
+        acc.visits += (unsigned long long)found.popc();
+        acc_lanes<W>(acc, found);
+        deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+        claimed = true;
+      }
+    }
+    ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+  }
+}
+
+// After a push round: the vertices it queued merge their new lanes into vis.
+template <int W>
+__device__ void lg_push_merge(const MsParams &p, int L, const uint64_t *nxt, MsRound *Rn,
+                              MsAcc &acc) {
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int next_parity = (L + 1) & 1;
+  const int32_t *q = next_parity ? p.queue1 : p.queue0;
+  const int64_t nl = *(volatile unsigned *)&Rn->res_light;
+  const int64_t nbg = *(volatile unsigned *)&Rn->res_big;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nl + nbg; j += nthreads) {
+    const int64_t v = j < nl ? q[j] : q[p.n - 1 - (j - nl)];
+    const Mask<W> nw = ld_mask<W>(nxt, v);
+    st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
+    acc.visits += (unsigned long long)nw.popc();
+    acc_lanes<W>(acc, nw);
+  }
+}
+
+// End of round L (last block to arrive): as the direct kernel's, plus the
+// history bound -- round L + 1 writes F_{L+2}, which must be a plane.
+template <int W>
+__device__ unsigned lg_decide(const MsParams &p, int L, int dir, int ran) {
+  MsCtl *ctl = p.ctl;
+  const MsRound *Rn = &ctl->rec[(L + 1) % kRing];
+  unsigned long long nf = 0, visits = 0, mf = 0;
+#pragma unroll
+  for (int i = 0; i < kCounterShards; ++i) {
+    nf += *(volatile const unsigned long long *)&Rn->nf[i];
+    visits += *(volatile const unsigned long long *)&Rn->visits[i];
+    mf += *(volatile const unsigned long long *)&Rn->mf[i];
+  }
+  cg_stats *st = p.stats;
+  const long long now = global_ns();
+  if (ran < CG_HISTORY) {
+    st->nf_history[ran] = (int64_t)visits;
+    st->direction_history[ran] = dir;
+    st->round_ns[ran] = now - ctl->t_round;
+  }
+  ctl->t_round = now;
+  if (dir == 1) ctl->pull_rounds += 1;
+  ctl->visited += visits;
+  bool stop = nf == 0;
+  if (!stop && L + 1 >= p.level_cap) {
+    atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
+    stop = true;
+  }
+  if (!stop && L + 2 >= p.hist_planes) {
+    *(volatile int *)p.flag = 1;  // outgrew the history: the direct kernel takes over
+    stop = true;
+  }
+  int next;
+  if (p.direction == CG_DIR_TOPDOWN)
+    next = 0;
+  else if (p.direction == CG_DIR_BOTTOMUP)
+    next = 1;
+  else
+    next = ((double)mf * (double)p.ms_alpha > (double)p.nnz) ? 1 : 0;
+  if (next != dir) ctl->switches += 1;
+  ctl->L = L + 1;
+  ctl->dir = next;
+  MsRound *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
+  for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->visits[i] = Rz->mf[i] = 0;
+  Rz->big = 0;
+  Rz->res_light = Rz->res_big = 0;
+  Rz->nlight = Rz->work = 0;
+  Rz->lanes[0] = Rz->lanes[1] = 0;
+  if (stop) {
+    const int rounds = ran + 1;
+    st->status = *(volatile int *)&ctl->status;
+    st->rounds = rounds;
+    st->visited = (int64_t)ctl->visited;
+    st->pull_rounds = ctl->pull_rounds;
+    st->switches = ctl->switches;
+    st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
+    st->device_ms = 0.f;
+  }
+  return (stop ? kMsStop : 0u) | (next ? kMsNextPull : 0u);
+}
+
+template <int W>
+struct LgRoundDecision {
+  const MsParams *p;
+  int L, dir, ran;
+  __device__ unsigned operator()() const { return lg_decide<W>(*p, L, dir, ran); }
+};
+
+struct LgResolveSnapshot {
+  MsRound *R;
+  __device__ unsigned operator()() const {
+    R->res_light = *(volatile unsigned *)&R->nlight;
+    R->res_big = (unsigned)(*(volatile unsigned long long *)&R->big >> 32);
+    return 0u;
+  }
+};
+
+struct LgSetupDecision {
+  MsCtl *ctl;
+  cg_stats *st;
+  __device__ unsigned operator()() const {
+    const long long now = global_ns();
+    st->setup_ns = now - ctl->t_start;
+    st->finish_ns = 0;
+    ctl->t_round = now;
+    return 0u;
+  }
+};
+
+// The rounds of one batch (cooperative, persistent): roots[0..k) seeded in
+// F_0; round L reads F_L, writes F_{L+1} and clears F_{L+2}.
+template <int W>
+__global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
+  __shared__ unsigned s_payload;
+  MsCtl *ctl = p.ctl;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t_start = global_ns();
+  uint64_t *f0 = plane<W>(p, 0), *f1 = plane<W>(p, 1);
+  for (int64_t i = gtid; i < p.n * W; i += nthreads) {
+    p.vis[i] = 0;
+    f0[i] = 0;
+    f1[i] = 0;
+  }
+  for (int64_t w = gtid; w < p.words; w += nthreads) {
+    p.touched0[w] = 0;
+    p.touched1[w] = 0;
+  }
+  bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
+  if (ok && blockIdx.x == 0 && threadIdx.x < p.k) {
+    const int i = threadIdx.x;
+    const int32_t r = p.roots[i];
+    const unsigned long long bit = 1ull << (i & 63);
+    atomicOr(reinterpret_cast<unsigned long long *>(p.vis + (int64_t)r * W + (i >> 6)), bit);
+    atomicOr(reinterpret_cast<unsigned long long *>(f0 + (int64_t)r * W + (i >> 6)), bit);
+    bool first = true;
+    for (int j = 0; j < i; ++j) first = first && (p.roots[j] != r);
+    if (first) {
+      const int64_t deg = p.out_off[r + 1] - p.out_off[r];
+      MsRound *R0 = &ctl->rec[0];
+      if (deg <= kLightMax) {
+        p.queue0[atomicAdd(&R0->nlight, 1u)] = r;
+      } else {
+        const unsigned long long old = atomicAdd(&R0->big, (1ull << 32) | (unsigned long long)deg);
+        p.queue0[p.n - 1 - (int64_t)(old >> 32)] = r;
+        p.bigoff0[old >> 32] = (unsigned)old;
+      }
+      atomicAdd(&R0->nf[0], 1ull);
+      atomicAdd(&R0->mf[0], (unsigned long long)deg);
+    }
+    if (i == 0) {
+      const Mask<W> a0 = lane_mask<W>(p.k);
+      ctl->rec[0].lanes[0] = a0.w[0];
+      ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
+      ctl->visited = (unsigned long long)p.k;
+    }
+  }
+  if (ok) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                  LgSetupDecision{ctl, p.stats});
+    __syncthreads();
+    ok = s_payload != kWaitFailed;
+  }
+  int L = 0, dir = 0, ran = 0;
+  MsAcc acc, tot;
+  while (ok) {
+    const uint64_t *cur = plane<W>(p, L);
+    uint64_t *nxt = plane<W>(p, L + 1);
+    uint32_t *touched = (L & 1) ? p.touched1 : p.touched0;
+    uint32_t *touched_next = (L & 1) ? p.touched0 : p.touched1;
+    MsRound *Rc = &ctl->rec[L % kRing];
+    MsRound *Rn = &ctl->rec[(L + 1) % kRing];
+    if (L + 2 < p.hist_planes) {
+      uint64_t *clr = plane<W>(p, L + 2);
+      for (int64_t i = gtid; i < p.n * W; i += nthreads) clr[i] = 0;
+    }
+    for (int64_t w = gtid; w < p.words; w += nthreads) touched_next[w] = 0;
+    if (dir == 1) {
+      Mask<W> active;
+#pragma unroll
+      for (int i = 0; i < W; ++i) active.w[i] = *(volatile unsigned long long *)&Rc->lanes[i];
+      lg_pull<W>(p, L, cur, nxt, active, Rn, acc);
+      if (p.nhub > 0) {
+        if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
+        lg_hub_merge<W>(p, L, nxt, Rn, acc);
+      }
+    } else {
+      ms_push<W, true>(p, L, cur, nxt, touched, Rc, Rn, acc);
+      __syncthreads();
+      if (threadIdx.x == 0)
+        s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                    LgResolveSnapshot{Rn});
+      __syncthreads();
+      if (s_payload == kWaitFailed) {
+        ok = false;
+        break;
+      }
+      lg_push_merge<W>(p, L, nxt, Rn, acc);
+    }
+    ms_block_totals(acc, tot);
+    if (threadIdx.x == 0) {
+      const int sh = blockIdx.x % kCounterShards;
+      if (tot.nf) atomicAdd(&Rn->nf[sh], tot.nf);
+      if (tot.visits) atomicAdd(&Rn->visits[sh], tot.visits);
+      if (tot.mf) atomicAdd(&Rn->mf[sh], tot.mf);
+      if (tot.lanes[0]) atomicOr(&Rn->lanes[0], tot.lanes[0]);
+      if (tot.lanes[1]) atomicOr(&Rn->lanes[1], tot.lanes[1]);
+      s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
+                                  LgRoundDecision<W>{&p, L, dir, ran});
+    }
+    __syncthreads();
+    const unsigned payload = s_payload;
+    if (payload == kWaitFailed) {
+      ok = false;
+      break;
+    }
+    if (payload & kMsStop) break;
+    dir = (payload & kMsNextPull) ? 1 : 0;
+    ++L;
+    ++ran;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !ok)
+    p.stats->status = *(volatile int *)&ctl->status;
+}
+
+// ---- output pass ----------------------------------------------------------
+
+// Up to kOutLevels levels >= `from` holding lanes of `todo` at vertex v (half
+// h of the lanes), ascending: Ls[k] the level, Ms[k] its lanes.  Advances
+// `from` past the last one taken; returns the lanes taken.
+template <int W>
+__device__ __forceinline__ uint64_t collect_levels(const MsParams &p, int64_t v, int h, int rounds,
+                                                   uint64_t todo, int &from, int (&Ls)[kOutLevels],
+                                                   uint64_t (&Ms)[kOutLevels]) {
+#pragma unroll
+  for (int k = 0; k < kOutLevels; ++k) {
+    Ls[k] = 1;
+    Ms[k] = 0;
+  }
+  uint64_t covered = 0;
+  int nl = 0;
+  for (int L = from; L < rounds && nl < kOutLevels && todo; ++L) {
+    const uint64_t m = plane<W>(p, L)[v * W + h] & todo;
+    if (m) {
+#pragma unroll
+      for (int k = 0; k < kOutLevels; ++k)
+        if (k == nl) {
+          Ls[k] = L;
+          Ms[k] = m;
+        }
+      covered |= m;
+      todo &= ~m;
+      ++nl;
+    }
+    from = L + 1;
+  }
+  return covered;
+}
+
+// Lanes of `want` for which u is one level closer to the root than v: bit l
+// of Ms[k] is a lane with v at level Ls[k]; u qualifies if F_{Ls[k]-1}[u] has l.
+template <int W>
+__device__ __forceinline__ uint64_t parent_hits(const MsParams &p, int32_t u, int h,
+                                                const int (&Ls)[kOutLevels],
+                                                const uint64_t (&Ms)[kOutLevels], uint64_t want) {
+  uint64_t b = 0;
+#pragma unroll
+  for (int k = 0; k < kOutLevels; ++k)
+    if (Ms[k] & want) b |= Ms[k] & plane<W>(p, Ls[k] - 1)[(int64_t)u * W + h];
+  return b & want;
+}
+
+// 32 x 32 bit-matrix transpose across the warp: lane r holds row r (bit c =
+// entry (r, c)); afterwards lane t holds column t (bit r = entry (r, t)).
+// Five butterfly steps, each swapping off-diagonal blocks with the partner
+// lane t ^ j.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const uint32_t m = j == 16 ? 0x0000ffffu
+                     : j == 8  ? 0x00ff00ffu
+                     : j == 4  ? 0x0f0f0f0fu
+                     : j == 2  ? 0x33333333u
+                               : 0x55555555u;
+    const uint32_t y = __shfl_xor_sync(kMsFull, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y & ~m) >> j)) : ((x & m) | ((y & m) << j));
+  }
+  return x;
+}
+
+// The whole warp scans in-list entries [s, e) (same arguments in every lane)
+// for the first hit of each lane of `want`, 4 x 32 entries per step with all
+// their loads in flight, taken 32 at a time in ascending order.  The 32 x 64
+// hit matrix of a sub-step (entries x lanes) is transposed so that warp lane
+// t owns lanes t and t + 32: its first set bit is the first (smallest) entry
+// holding that lane, and it calls sink(lane, u) for each of its two lanes
+// found -- every warp lane at once.  Returns the lanes not found.
+template <int W, class Sink>
+__device__ __forceinline__ uint64_t warp_parent_scan(const MsParams &p, int64_t s, int64_t e,
+                                                     int h, const int (&Ls)[kOutLevels],
+                                                     const uint64_t (&Ms)[kOutLevels],
+                                                     uint64_t want, Sink sink) {
+  constexpr int G = 4;
+  const int lane = lane_id();
+  for (int64_t base = s; base < e && want; base += 32 * G) {
+    int32_t u[G];
+    uint64_t b[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const int64_t i = base + 32 * k + lane;
+      u[k] = i < e ? __ldg(p.in_idx + i) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < G; ++k) b[k] = u[k] >= 0 ? parent_hits<W>(p, u[k], h, Ls, Ms, want) : 0;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const uint64_t bk = b[k] & want;
+      if (!__ballot_sync(kMsFull, bk != 0)) continue;
+      const uint32_t lo = warp_transpose32((uint32_t)bk);
+      const uint32_t hi = warp_transpose32((uint32_t)(bk >> 32));
+      const uint64_t found = (uint64_t)__ballot_sync(kMsFull, lo != 0) |
+                             ((uint64_t)__ballot_sync(kMsFull, hi != 0) << 32);
+      const int32_t plo = __shfl_sync(kMsFull, u[k], lo ? __ffs(lo) - 1 : 0);
+      const int32_t phi = __shfl_sync(kMsFull, u[k], hi ? __ffs(hi) - 1 : 0);
+      if (lo) sink(lane, plo);
+      if (hi) sink(lane + 32, phi);
+      want &= ~found;
+    }
+  }
+  return want;
+}
+
+// Phase 1 of the output pass: parents of the vertices of in-degree >
+// kPullLight (one candidate slot each).  Their in-lists are cut into
+// kHubChunk-entry chunks, scanned by different warps; each chunk's first hit
+// per lane goes to the slot by atomicMin, so the slot ends with the lowest
+// in-neighbour one level closer, whichever chunk holds it.
+template <int W>
+__global__ void __launch_bounds__(kOutBlock, 3) msbfs_cand_parents(MsParams p) {
+  MsCtl *ctl = p.ctl;
+  if (*(volatile int *)p.flag || *(volatile int *)&ctl->status != 0 || p.ncand == 0) return;
+  int rounds = *(volatile int *)&ctl->L;
+  if (rounds > p.hist_planes) rounds = p.hist_planes;
+  // levels whose round was a push round already have their parents (ms_relax);
+  // level L came from round L - 1
+  uint64_t pulled = 0;
+  for (int L = 2; L < rounds && L <= 64; ++L)
+    if (p.stats->direction_history[L - 1] == 1) pulled |= 1ull << (L - 1);
+  if (!pulled) return;
+  const unsigned nchunks = p.cand_choff[p.ncand];
+  const unsigned nwarps = gridDim.x * kOutWarps;
+  // slots 0 .. nmed - 1 are the medium vertices, one chunk each (chunk c is
+  // slot c); the hubs' chunks follow
+  const unsigned nmed = (unsigned)p.nmed;
+  for (unsigned c = blockIdx.x * kOutWarps + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
+    unsigned lo = c < nmed ? c : nmed, hi = c < nmed ? c : (unsigned)p.ncand - 1;
+    while (lo < hi) {
+      const unsigned mid = (lo + hi + 1) >> 1;
+      if (p.cand_choff[mid] <= c)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int slot = (int)lo;
+    const int32_t v = p.cand_vtx[slot];
+    const int64_t v_beg = __ldg(p.in_off + v), v_end = __ldg(p.in_off + v + 1);
+    const int64_t s = v_beg + (int64_t)(c - p.cand_choff[slot]) * kHubChunk;
+    const int64_t e = min(s + (int64_t)kHubChunk, v_end);
+    const bool single = s == v_beg && e == v_end;
+    for (int h = 0; h < W && 64 * h < p.k; ++h) {
+      uint32_t *cand = p.cand + (int64_t)slot * (64 * W) + 64 * h;
+      // the vertex's masks of levels 2 .. rounds - 1, 32 levels at a time
+      // (lane j holds level L0 + j), taken kOutLevels nonzero levels per scan
+      for (int L0 = 2; L0 < rounds; L0 += 32) {
+        const int L = L0 + lane_id();
+        const bool want = L < rounds && L <= 64 && ((pulled >> (L - 1)) & 1ull);
+        const uint64_t m = want ? plane<W>(p, L)[(int64_t)v * W + h] : 0ull;
+        unsigned have = __ballot_sync(kMsFull, m != 0ull);
+        while (have) {
+          int Ls[kOutLevels];
+          uint64_t Ms[kOutLevels];
+          uint64_t covered = 0;
+#pragma unroll
+          for (int k = 0; k < kOutLevels; ++k) {
+            const int j = have ? __ffs(have) - 1 : 0;
+            const uint64_t mk = __shfl_sync(kMsFull, m, j);
+            Ls[k] = have ? L0 + j : 1;
+            Ms[k] = have ? mk : 0ull;
+            covered |= Ms[k];
+            if (have) have &= have - 1;
+          }
+          if (single)  // the whole in-list is this chunk: nobody else writes the slot
+            warp_parent_scan<W>(p, s, e, h, Ls, Ms, covered,
+                                [&](int bit, int32_t u) { cand[bit] = (uint32_t)u; });
+          else
+            warp_parent_scan<W>(p, s, e, h, Ls, Ms, covered,
+                                [&](int bit, int32_t u) { atomicMin(cand + bit, (unsigned)u); });
+        }
+      }
+    }
+  }
+}
+
+// Phase 2.  Each warp takes 32 consecutive vertices (one per thread) and, per
+// 64-lane half of the batch, fills a shared tile: lvl[t][l] from the history
+// planes; par[t][l] = v for level 0, the lane's root for level 1, and for
+// deeper levels the slot's candidate (in-degree > kPullLight) or the first
+// hit of the thread's own scan of its (at most kPullLight-entry) in-list.
+// Then it writes, per lane l, the tile's 32 levels and 32 parents as two
+// 128-byte rows.
+template <int W>
+__global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
+  extern __shared__ __align__(16) unsigned char s_tile[];
+  constexpr int kPre = 8;    // history planes loaded together
+  constexpr int kScanG = 8;  // in-list entries loaded together
+  MsCtl *ctl = p.ctl;
+  if (*(volatile int *)p.flag) {
+    // the gated direct launch that follows needs a clean control block
+    if (blockIdx.x == 0) {
+      unsigned long long *c = reinterpret_cast<unsigned long long *>(ctl);
+      for (int i = threadIdx.x; i < (int)(sizeof(MsCtl) / 8); i += blockDim.x) c[i] = 0ull;
+    }
+    return;
+  }
+  if (*(volatile int *)&ctl->status != 0) return;  // timed out or over the level cap
+  int rounds = *(volatile int *)&ctl->L;           // F_0 .. F_rounds, F_rounds empty
+  if (rounds > p.hist_planes) rounds = p.hist_planes;
+  const int lane = lane_id();
+  const int wib = threadIdx.x >> 5;
+  int32_t *par = reinterpret_cast<int32_t *>(s_tile + wib * kOutWarpBytes);
+  uint8_t *lvl = s_tile + wib * kOutWarpBytes + 32 * kParStride * 4;
+  int32_t *my_par = par + lane * kParStride;
+  uint8_t *my_lvl = lvl + lane * kLvlStride;
+  const int64_t nwarps = (int64_t)gridDim.x * kOutWarps;
+  for (int64_t tile = (int64_t)blockIdx.x * kOutWarps + wib; tile * 32 < p.n; tile += nwarps) {
+    const int64_t v = tile * 32 + lane;
+    const bool valid = v < p.n;
+    int64_t s = 0, e = 0;
+    int slot = -1;
+    if (valid) {
+      s = __ldg(p.in_off + v);
+      e = __ldg(p.in_off + v + 1);
+      slot = p.cand_slot[v];
+    }
+#pragma unroll 1
+    for (int h = 0; h < W && 64 * h < p.k; ++h) {
+      uint32_t *lw = reinterpret_cast<uint32_t *>(my_lvl);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) lw[i] = 0xffffffffu;
+      // levels >= 2 of a light vertex: the first kOutLevels nonzero ones here,
+      // any further ones (rare) through collect_levels below
+      int Ls[kOutLevels];
+      uint64_t Ms[kOutLevels];
+      int nl = 0;
+      uint64_t gtodo = 0, rest = 0;
+      int last = 1;
+#pragma unroll
+      for (int k = 0; k < kOutLevels; ++k) {
+        Ls[k] = 1;
+        Ms[k] = 0;
+      }
+      // parents of levels >= 2 of the tile's slotted vertices come from phase 1:
+      // the warp copies each slot's 256-byte row into the vertex's tile row, up
+      // to four rows' loads in flight
+      {
+        unsigned pend = __ballot_sync(kMsFull, slot >= 0);
+        while (pend) {
+          int src[4];
+          uint2 x[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            src[r] = pend ? __ffs(pend) - 1 : -1;
+            if (pend) pend &= pend - 1;
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const int ss = src[r] >= 0 ? __shfl_sync(kMsFull, slot, src[r]) : -1;
+            x[r] = ss >= 0 ? __ldg(reinterpret_cast<const uint2 *>(p.cand + (int64_t)ss * (64 * W) +
+                                                                  64 * h) + lane)
+                           : make_uint2(0u, 0u);
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            if (src[r] >= 0) {
+              par[src[r] * kParStride + 2 * lane] = (int32_t)x[r].x;
+              par[src[r] * kParStride + 2 * lane + 1] = (int32_t)x[r].y;
+            }
+          }
+        }
+        __syncwarp();
+      }
+      if (valid) {
+        for (int L0 = 0; L0 < rounds; L0 += kPre) {
+          uint64_t pm[kPre];
+#pragma unroll
+          for (int j = 0; j < kPre; ++j)
+            pm[j] = L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] : 0ull;
+#pragma unroll
+          for (int j = 0; j < kPre; ++j) {
+            uint64_t m = pm[j];
+            const int L = L0 + j;
+            if (m && L >= 2 && slot < 0) {
+              if (nl < kOutLevels) {
+#pragma unroll
+                for (int k = 0; k < kOutLevels; ++k)
+                  if (k == nl) {
+                    Ls[k] = L;
+                    Ms[k] = m;
+                  }
+                ++nl;
+                gtodo |= m;
+                last = L;
+              } else {
+                rest |= m;
+              }
+            }
+            while (m) {
+              const int b = __ffsll((long long)m) - 1;
+              m &= m - 1;
+              my_lvl[b] = (uint8_t)L;
+              if (L == 0)
+                my_par[b] = (int32_t)v;
+              else if (L == 1)
+                my_par[b] = p.roots[64 * h + b];
+            }
+          }
+        }
+      }
+      // light vertices: the whole in-list (<= kPullLight entries), kScanG
+      // entries' loads in flight, kOutLevels levels per pass
+      int from = last + 1;
+      while (gtodo) {
+        for (int64_t j0 = s; j0 < e && gtodo; j0 += kScanG) {
+          int32_t u[kScanG];
+          uint64_t b[kScanG];
+#pragma unroll
+          for (int k = 0; k < kScanG; ++k) u[k] = j0 + k < e ? __ldg(p.in_idx + j0 + k) : -1;
+#pragma unroll
+          for (int k = 0; k < kScanG; ++k)
+            b[k] = u[k] >= 0 ? parent_hits<W>(p, u[k], h, Ls, Ms, gtodo) : 0;
+#pragma unroll
+          for (int k = 0; k < kScanG; ++k) {
+            uint64_t bk = b[k] & gtodo;
+            gtodo &= ~bk;
+            while (bk) {
+              const int bit = __ffsll((long long)bk) - 1;
+              bk &= bk - 1;
+              my_par[bit] = u[k];
+            }
+          }
+        }
+        gtodo = 0;
+        if (rest) {  // more than kOutLevels levels at this vertex
+          gtodo = collect_levels<W>(p, v, h, rounds, rest, from, Ls, Ms);
+          rest &= ~gtodo;
+          if (!gtodo) rest = 0;
+        }
+      }
+      __syncwarp();
+      // rows: lane l of this half, vertices tile*32 .. tile*32 + 31
+      const int lanes = min(64, p.k - 64 * h);
+#pragma unroll 8
+      for (int l = 0; l < lanes; ++l) {
+        const uint8_t lv = lvl[lane * kLvlStride + l];
+        const int64_t at = (int64_t)(64 * h + l) * p.n + v;
+        if (valid) {
+          p.levels[at] = lv == 0xff ? -1 : (int32_t)lv;
+          p.parents[at] = lv == 0xff ? -1 : par[lane * kParStride + l];
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // the last block out records the time since the last round ended
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(&ctl->exited, 1u) + 1u == gridDim.x)
+    p.stats->finish_ns = global_ns() - *(volatile long long *)&ctl->t_round;
+}
+
+template <int W>
+int ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d_levels,
+                int32_t *d_parents) {
+  MsParams p = ms_params<W>(g, s);
+  p.levels = d_levels;
+  p.parents = d_parents;
+  p.k = k;
+  for (int i = 0; i < kMsMaxLanes; ++i) p.roots[i] = i < k ? (int32_t)roots[i] : 0;
+  int rc = ms_reset<W>(s, g->stream);
+  if (rc) return rc;
+  int block = g->opt.block_size > 0 ? g->opt.block_size : kMsBlock;
+  if (block > kMsBlock) block = kMsBlock;
+  block = (block / 32) * 32;
+  if (block < 128) block = 128;  // seeding uses threads 0..k-1 of block 0
+  int per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msbfs_ledger<W>, block, 0));
+  if (per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+  if (g->opt.blocks_per_sm > 0 && g->opt.blocks_per_sm < per_sm) per_sm = g->opt.blocks_per_sm;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(per_sm * g->num_sms);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = g->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CG_CUDA(cudaLaunchKernelEx(&cfg, msbfs_ledger<W>, p));
+  if (s->ncand > 0) {
+    int cand_per_sm = 0;
+    CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cand_per_sm, msbfs_cand_parents<W>,
+                                                          kOutBlock, 0));
+    if (cand_per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+    msbfs_cand_parents<W><<<cand_per_sm * g->num_sms, kOutBlock, 0, g->stream>>>(p);
+    CG_CUDA(cudaGetLastError());
+  }
+  const int smem = kOutWarps * kOutWarpBytes;
+  CG_CUDA(cudaFuncSetAttribute(msbfs_outputs<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem));
+  int out_per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out_per_sm, msbfs_outputs<W>, kOutBlock,
+                                                        smem));
+  if (out_per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+  const int64_t tiles = (g->n + 31) / 32;
+  int64_t blocks = (tiles + kOutWarps - 1) / kOutWarps;
+  const int64_t cap = (int64_t)out_per_sm * g->num_sms;
+  if (blocks > cap) blocks = cap;
+  msbfs_outputs<W><<<(unsigned)blocks, kOutBlock, smem, g->stream>>>(p);
+  CG_CUDA(cudaGetLastError());
+  return CG_OK;
+}
+
+}  // namespace
+
+int ms_ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d_levels,
+                   int32_t *d_parents) {
+  return s->lane_words == 2 ? ledger_pass<2>(g, s, roots, k, d_levels, d_parents)
+                            : ledger_pass<1>(g, s, roots, k, d_levels, d_parents);
+}
+
+}  // namespace cg

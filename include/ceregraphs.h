@@ -77,6 +77,9 @@ typedef struct cg_options {
   float ms_alpha;           /* multi-source: pull when frontier edges > nnz / ms_alpha */
   int32_t test_unmatched_wait; /* test hook: 1 makes the first grid-wide wait wait for an
                                   arrival that never comes, so it must time out */
+  int32_t ms_history;       /* multi-source: rounds of frontier history for the output
+                               pass (0 = as memory allows, at most 64; < 0 = none: outputs
+                               are written during the rounds) */
 } cg_options;
 
 #define CG_HISTORY 64

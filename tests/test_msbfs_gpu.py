@@ -134,3 +134,52 @@ def test_per_root_capture(built_lib, oracle_mod):
       assert np.array_equal(d_lv[i].cpu().numpy(), l)
       assert np.array_equal(d_pa[i].cpu().numpy(), p)
     exe.close()
+
+
+@pytest.mark.parametrize("history", [-1, 0, 3, 6])
+def test_msbfs_history_modes(built_lib, oracle_mod, history):
+  """Outputs written during the rounds (history < 0), from the round history
+  (0: as memory allows), and searches that outgrow a short history (3, 6:
+  the gated direct launch takes over) -- all equal to the oracle."""
+  cases = [(generators.rmat(13, 16, 7), None),
+           (generators.er_directed(12, 6, 9), [0, 1, 2, 500, 4095]),
+           (generators.grid2d(40), [0, 39, 820, 1599])]
+  for a, roots in cases:
+    if roots is None:
+      roots = graph500.pick_sources(a, 100, 4)
+    rl, rp, rounds = _oracle_all(oracle_mod, a, roots)
+    with Graph(a) as g:
+      for lw in (1, 2):
+        g.set_options(ms_history=history, lane_words=lw)
+        lv, pa, st = g.msbfs(roots)
+        assert st["status"] == 0
+        assert np.array_equal(lv, rl) and np.array_equal(pa, rp), (history, lw)
+        assert st["rounds"] == rounds
+
+
+def test_msbfs_history_overflow_in_a_captured_graph(built_lib, oracle_mod):
+  """A captured batch whose search outgrows the history: the fallback launch
+  is part of the graph and decides on the device."""
+  torch = pytest.importorskip("torch")
+  a = generators.grid2d(30)
+  roots = [0, 29, 450, 899]
+  rl, rp, _ = _oracle_all(oracle_mod, a, roots)
+  b = generators.rmat(12, 16, 0)
+  broots = graph500.pick_sources(b, 64, 2)
+  bl, bp, _ = _oracle_all(oracle_mod, b, broots)
+  for arr, rts, wl, wp in ((a, roots, rl, rp), (b, broots, bl, bp)):
+    with Graph(arr) as g:
+      g.set_options(ms_history=8)
+      d_lv = torch.empty((len(rts), arr.n), dtype=torch.int32, device="cuda")
+      d_pa = torch.empty_like(d_lv)
+      torch.cuda.synchronize()
+      g.msbfs_device(rts, d_lv, d_pa)
+      g.last_stats()
+      exe = g.capture(lambda: g.msbfs_device(rts, d_lv, d_pa))
+      d_lv.fill_(7)
+      d_pa.fill_(7)
+      torch.cuda.synchronize()
+      exe.launch()
+      assert g.last_stats()["status"] == 0
+      assert np.array_equal(d_lv.cpu().numpy(), wl) and np.array_equal(d_pa.cpu().numpy(), wp)
+      exe.close()
