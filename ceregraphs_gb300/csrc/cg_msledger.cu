@@ -1,25 +1,31 @@
 // Multi-source BFS with the outputs written after the search ("ledger"
-// mode).  The rounds advance only the W-word lane masks: vis, and the
-// frontier F_L of every round, kept as a history F_0 .. F_D in HBM.  Nothing
-// is written per (lane, vertex) while the rounds run.  One output pass after
-// the last round then writes every (lane, vertex) output exactly once:
+// mode).  The rounds advance the W-word lane masks -- vis, and the frontier
+// F_L of every round, kept as a history F_0 .. F_D in HBM -- and write no
+// per-(lane, vertex) output.  One output pass after the last round writes
+// every (lane, vertex) output exactly once:
 //   level(l, v)  = the round L whose F_L[v] holds bit l      (-1 if none)
-//   parent(l, v) = roots[l] if level 1, else the lowest in-neighbour u of v
-//                  with bit l in F_{level - 1}[u]
+//   parent(l, v) = v at level 0, roots[l] at level 1, else the lowest
+//                  in-neighbour u of v with bit l in F_{level - 1}[u]
 // which is the lowest-index rule of the per-root search and of the direct
 // batched kernel (bfs/README.md:208-224), so the outputs are identical.
 //
 // Why: written during the rounds, every discovery is a 4-byte store into one
 // of 64 rows -- 32 scattered stores per warp instruction, each a separate L1
 // wavefront and L2 transaction, and sectors completed across rounds (partial
-// sector writes).  Here the output pass stages a 32-vertex x 64-lane tile per
-// warp in shared memory and writes each lane's 32 values as one 128-byte row.
+// sector writes).  Here the output pass writes, lane by lane, the 32 values of
+// a warp's 32 consecutive vertices as one 128-byte row.
+//
+// Parents: vertices of in-degree > kPullLight have a slot of 64 W parent
+// candidates.  A push round relaxing u -> v takes atomicMin(slot[l], u) for
+// each new lane l (ms_relax); a pull round scans such a vertex's ascending
+// in-list with one warp (or its chunks, for hubs, with several) and records
+// each lane's first hit (or_warp_first).  Vertices of smaller in-degree are
+// resolved in the output pass by their thread's scan of their short in-list.
 //
 // Rounds: a pull round ORs the frontier masks of a vertex's in-neighbours
-// until every wanted lane is found (no order needed: parents come later); a
-// push round ORs frontier masks into out-neighbours' next masks with
-// atomicOr, then merges them into vis.  Hubs' in-lists are split into chunks
-// across warps as in the direct kernel.
+// until every wanted lane is found; a push round ORs frontier masks into
+// out-neighbours' next masks with atomicOr, then merges them into vis.  Hubs'
+// in-lists are split into chunks across warps as in the direct kernel.
 //
 // A search that needs more rounds than the history holds sets a flag and
 // stops; the output pass then only clears the control block, and the direct
@@ -63,27 +69,72 @@ __device__ __forceinline__ Mask<W> or_thread(const MsParams &p, int64_t s, int64
   return got;
 }
 
-// The same by a whole warp (all lanes call with the same arguments), 4 x 32
-// entries per step.
+// 32 x 32 bit-matrix transpose across the warp: lane r holds row r (bit c =
+// entry (r, c)); afterwards lane t holds column t (bit r = entry (r, t)).
+// Five butterfly steps, each swapping off-diagonal blocks with the partner
+// lane t ^ j.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const uint32_t m = j == 16 ? 0x0000ffffu
+                     : j == 8  ? 0x00ff00ffu
+                     : j == 4  ? 0x0f0f0f0fu
+                     : j == 2  ? 0x33333333u
+                               : 0x55555555u;
+    const uint32_t y = __shfl_xor_sync(kMsFull, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y & ~m) >> j)) : ((x & m) | ((y & m) << j));
+  }
+  return x;
+}
+
+// or_warp that also records, per lane of `want`, the first in-list entry
+// holding it -- the lowest-index parent -- into row[lane] (plain stores when
+// the warp scans the whole in-list, atomicMin when other warps scan other
+// chunks of it).  The hits of 32 entries form a 32 x 64 W bit matrix that is
+// transposed a word at a time, so warp lane t resolves lanes t and t + 32 of
+// each word at once.
 template <int W>
-__device__ __forceinline__ Mask<W> or_warp(const MsParams &p, int64_t s, int64_t e,
-                                           const Mask<W> &want, const uint64_t *cur) {
+__device__ __forceinline__ Mask<W> or_warp_first(const MsParams &p, int64_t s, int64_t e,
+                                                 const Mask<W> &want, const uint64_t *cur,
+                                                 uint32_t *row, bool atomic) {
   constexpr int G = 4;
   const int lane = lane_id();
   Mask<W> got = Mask<W>::zero();
   for (int64_t base = s; base < e; base += 32 * G) {
     int32_t u[G];
+    Mask<W> f[G];
 #pragma unroll
     for (int k = 0; k < G; ++k) {
       const int64_t i = base + 32 * k + lane;
       u[k] = i < e ? __ldg(p.in_idx + i) : -1;
     }
-    Mask<W> f = Mask<W>::zero();
 #pragma unroll
-    for (int k = 0; k < G; ++k)
-      if (u[k] >= 0) f = f | ld_mask<W>(cur, u[k]);
-    got = got | warp_or<W>(f & want);
-    if (got == want) break;
+    for (int k = 0; k < G; ++k) f[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const Mask<W> fk = (f[k] & want).andnot(got);
+      const Mask<W> F = warp_or<W>(fk);
+      if (!F.any()) continue;
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        if (!F.w[j]) continue;
+        const uint32_t lo = warp_transpose32((uint32_t)fk.w[j]);
+        const uint32_t hi = warp_transpose32((uint32_t)(fk.w[j] >> 32));
+        const int32_t plo = __shfl_sync(kMsFull, u[k], lo ? __ffs(lo) - 1 : 0);
+        const int32_t phi = __shfl_sync(kMsFull, u[k], hi ? __ffs(hi) - 1 : 0);
+        uint32_t *r = row + 64 * j;
+        if (atomic) {
+          if (lo) atomicMin(r + lane, (unsigned)plo);
+          if (hi) atomicMin(r + lane + 32, (unsigned)phi);
+        } else {
+          if (lo) r[lane] = (uint32_t)plo;
+          if (hi) r[lane + 32] = (uint32_t)phi;
+        }
+      }
+      got = got | F;
+      if (got == want) return got;
+    }
   }
   return got;
 }
@@ -133,7 +184,9 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     const Mask<W> seen = ld_mask<W>(p.vis, v);
     const Mask<W> want = active.andnot(seen);
     if (!want.any()) continue;
-    const Mask<W> got = or_warp<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1), want, cur);
+    // medium vertex j has candidate slot j: its parents of this round go there
+    const Mask<W> got = or_warp_first<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1), want,
+                                         cur, p.cand + j * (64 * W), false);
     const bool claimed = lane_id() == 0 && got.any();
     int64_t deg = 0;
     if (claimed) {
@@ -162,7 +215,9 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     if (!want.any()) continue;
     const int64_t s = __ldg(p.in_off + v) + (int64_t)(c - p.hub_choff[h]) * kHubChunk;
     const int64_t e = min(s + (int64_t)kHubChunk, __ldg(p.in_off + v + 1));
-    const Mask<W> got = or_warp<W>(p, s, e, want, cur);
+    // hub h has candidate slot nmed + h; several warps scan its chunks
+    const Mask<W> got = or_warp_first<W>(p, s, e, want, cur,
+                                         p.cand + (p.nmed + h) * (64 * W), true);
     if (lane_id() == 0) {
 #pragma unroll
       for (int j = 0; j < W; ++j)
@@ -476,150 +531,19 @@ __device__ __forceinline__ uint64_t parent_hits(const MsParams &p, int32_t u, in
   return b & want;
 }
 
-// 32 x 32 bit-matrix transpose across the warp: lane r holds row r (bit c =
-// entry (r, c)); afterwards lane t holds column t (bit r = entry (r, t)).
-// Five butterfly steps, each swapping off-diagonal blocks with the partner
-// lane t ^ j.
-__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
-  const int lane = lane_id();
-#pragma unroll
-  for (int j = 16; j > 0; j >>= 1) {
-    const uint32_t m = j == 16 ? 0x0000ffffu
-                     : j == 8  ? 0x00ff00ffu
-                     : j == 4  ? 0x0f0f0f0fu
-                     : j == 2  ? 0x33333333u
-                               : 0x55555555u;
-    const uint32_t y = __shfl_xor_sync(kMsFull, x, j);
-    x = (lane & j) ? ((x & ~m) | ((y & ~m) >> j)) : ((x & m) | ((y & m) << j));
-  }
-  return x;
-}
-
-// The whole warp scans in-list entries [s, e) (same arguments in every lane)
-// for the first hit of each lane of `want`, 4 x 32 entries per step with all
-// their loads in flight, taken 32 at a time in ascending order.  The 32 x 64
-// hit matrix of a sub-step (entries x lanes) is transposed so that warp lane
-// t owns lanes t and t + 32: its first set bit is the first (smallest) entry
-// holding that lane, and it calls sink(lane, u) for each of its two lanes
-// found -- every warp lane at once.  Returns the lanes not found.
-template <int W, class Sink>
-__device__ __forceinline__ uint64_t warp_parent_scan(const MsParams &p, int64_t s, int64_t e,
-                                                     int h, const int (&Ls)[kOutLevels],
-                                                     const uint64_t (&Ms)[kOutLevels],
-                                                     uint64_t want, Sink sink) {
-  constexpr int G = 4;
-  const int lane = lane_id();
-  for (int64_t base = s; base < e && want; base += 32 * G) {
-    int32_t u[G];
-    uint64_t b[G];
-#pragma unroll
-    for (int k = 0; k < G; ++k) {
-      const int64_t i = base + 32 * k + lane;
-      u[k] = i < e ? __ldg(p.in_idx + i) : -1;
-    }
-#pragma unroll
-    for (int k = 0; k < G; ++k) b[k] = u[k] >= 0 ? parent_hits<W>(p, u[k], h, Ls, Ms, want) : 0;
-#pragma unroll
-    for (int k = 0; k < G; ++k) {
-      const uint64_t bk = b[k] & want;
-      if (!__ballot_sync(kMsFull, bk != 0)) continue;
-      const uint32_t lo = warp_transpose32((uint32_t)bk);
-      const uint32_t hi = warp_transpose32((uint32_t)(bk >> 32));
-      const uint64_t found = (uint64_t)__ballot_sync(kMsFull, lo != 0) |
-                             ((uint64_t)__ballot_sync(kMsFull, hi != 0) << 32);
-      const int32_t plo = __shfl_sync(kMsFull, u[k], lo ? __ffs(lo) - 1 : 0);
-      const int32_t phi = __shfl_sync(kMsFull, u[k], hi ? __ffs(hi) - 1 : 0);
-      if (lo) sink(lane, plo);
-      if (hi) sink(lane + 32, phi);
-      want &= ~found;
-    }
-  }
-  return want;
-}
-
-// Phase 1 of the output pass: parents of the vertices of in-degree >
-// kPullLight (one candidate slot each).  Their in-lists are cut into
-// kHubChunk-entry chunks, scanned by different warps; each chunk's first hit
-// per lane goes to the slot by atomicMin, so the slot ends with the lowest
-// in-neighbour one level closer, whichever chunk holds it.
-template <int W>
-__global__ void __launch_bounds__(kOutBlock, 3) msbfs_cand_parents(MsParams p) {
-  MsCtl *ctl = p.ctl;
-  if (*(volatile int *)p.flag || *(volatile int *)&ctl->status != 0 || p.ncand == 0) return;
-  int rounds = *(volatile int *)&ctl->L;
-  if (rounds > p.hist_planes) rounds = p.hist_planes;
-  // levels whose round was a push round already have their parents (ms_relax);
-  // level L came from round L - 1
-  uint64_t pulled = 0;
-  for (int L = 2; L < rounds && L <= 64; ++L)
-    if (p.stats->direction_history[L - 1] == 1) pulled |= 1ull << (L - 1);
-  if (!pulled) return;
-  const unsigned nchunks = p.cand_choff[p.ncand];
-  const unsigned nwarps = gridDim.x * kOutWarps;
-  // slots 0 .. nmed - 1 are the medium vertices, one chunk each (chunk c is
-  // slot c); the hubs' chunks follow
-  const unsigned nmed = (unsigned)p.nmed;
-  for (unsigned c = blockIdx.x * kOutWarps + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
-    unsigned lo = c < nmed ? c : nmed, hi = c < nmed ? c : (unsigned)p.ncand - 1;
-    while (lo < hi) {
-      const unsigned mid = (lo + hi + 1) >> 1;
-      if (p.cand_choff[mid] <= c)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const int slot = (int)lo;
-    const int32_t v = p.cand_vtx[slot];
-    const int64_t v_beg = __ldg(p.in_off + v), v_end = __ldg(p.in_off + v + 1);
-    const int64_t s = v_beg + (int64_t)(c - p.cand_choff[slot]) * kHubChunk;
-    const int64_t e = min(s + (int64_t)kHubChunk, v_end);
-    const bool single = s == v_beg && e == v_end;
-    for (int h = 0; h < W && 64 * h < p.k; ++h) {
-      uint32_t *cand = p.cand + (int64_t)slot * (64 * W) + 64 * h;
-      // the vertex's masks of levels 2 .. rounds - 1, 32 levels at a time
-      // (lane j holds level L0 + j), taken kOutLevels nonzero levels per scan
-      for (int L0 = 2; L0 < rounds; L0 += 32) {
-        const int L = L0 + lane_id();
-        const bool want = L < rounds && L <= 64 && ((pulled >> (L - 1)) & 1ull);
-        const uint64_t m = want ? plane<W>(p, L)[(int64_t)v * W + h] : 0ull;
-        unsigned have = __ballot_sync(kMsFull, m != 0ull);
-        while (have) {
-          int Ls[kOutLevels];
-          uint64_t Ms[kOutLevels];
-          uint64_t covered = 0;
-#pragma unroll
-          for (int k = 0; k < kOutLevels; ++k) {
-            const int j = have ? __ffs(have) - 1 : 0;
-            const uint64_t mk = __shfl_sync(kMsFull, m, j);
-            Ls[k] = have ? L0 + j : 1;
-            Ms[k] = have ? mk : 0ull;
-            covered |= Ms[k];
-            if (have) have &= have - 1;
-          }
-          if (single)  // the whole in-list is this chunk: nobody else writes the slot
-            warp_parent_scan<W>(p, s, e, h, Ls, Ms, covered,
-                                [&](int bit, int32_t u) { cand[bit] = (uint32_t)u; });
-          else
-            warp_parent_scan<W>(p, s, e, h, Ls, Ms, covered,
-                                [&](int bit, int32_t u) { atomicMin(cand + bit, (unsigned)u); });
-        }
-      }
-    }
-  }
-}
-
-// Phase 2.  Each warp takes 32 consecutive vertices (one per thread) and, per
-// 64-lane half of the batch, fills a shared tile: lvl[t][l] from the history
-// planes; par[t][l] = v for level 0, the lane's root for level 1, and for
-// deeper levels the slot's candidate (in-degree > kPullLight) or the first
-// hit of the thread's own scan of its (at most kPullLight-entry) in-list.
-// Then it writes, per lane l, the tile's 32 levels and 32 parents as two
-// 128-byte rows.
+// Output pass.  Each warp takes 32 consecutive vertices (one per thread).  Per
+// 64-lane half of the batch a thread reads its vertex's history masks once
+// and records each lane's level as a byte of a shared tile row (0xFF =
+// unreached); parents of levels >= 2 go to a second tile: the slot's
+// candidates (in-degree > kPullLight, copied by the warp) or the first hit of
+// the thread's scan of its own short in-list.  Then, lane by lane, the warp
+// writes the tile's 32 levels and 32 parents as two 128-byte rows; parents of
+// levels 0 and 1 are the vertex and the lane's root.
 template <int W>
 __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   extern __shared__ __align__(16) unsigned char s_tile[];
-  constexpr int kPre = 8;    // history planes loaded together
-  constexpr int kScanG = 8;  // in-list entries loaded together
+  constexpr int kPre = 8;     // history planes loaded together
+  constexpr int kScanG = 8;   // in-list entries loaded together
   MsCtl *ctl = p.ctl;
   if (*(volatile int *)p.flag) {
     // the gated direct launch that follows needs a clean control block
@@ -651,24 +575,9 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
     }
 #pragma unroll 1
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
-      uint32_t *lw = reinterpret_cast<uint32_t *>(my_lvl);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) lw[i] = 0xffffffffu;
-      // levels >= 2 of a light vertex: the first kOutLevels nonzero ones here,
-      // any further ones (rare) through collect_levels below
-      int Ls[kOutLevels];
-      uint64_t Ms[kOutLevels];
-      int nl = 0;
-      uint64_t gtodo = 0, rest = 0;
-      int last = 1;
-#pragma unroll
-      for (int k = 0; k < kOutLevels; ++k) {
-        Ls[k] = 1;
-        Ms[k] = 0;
-      }
-      // parents of levels >= 2 of the tile's slotted vertices come from phase 1:
-      // the warp copies each slot's 256-byte row into the vertex's tile row, up
-      // to four rows' loads in flight
+      // parents of levels >= 2 of the tile's slotted vertices: the warp copies
+      // each slot's 256-byte candidate row into the vertex's tile row, four
+      // rows' loads in flight
       {
         unsigned pend = __ballot_sync(kMsFull, slot >= 0);
         while (pend) {
@@ -694,7 +603,21 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
             }
           }
         }
-        __syncwarp();
+      }
+      // level bytes; the first kOutLevels levels >= 2 of a light vertex for its
+      // scan, any further ones (rare) through collect_levels below
+      uint32_t *lw = reinterpret_cast<uint32_t *>(my_lvl);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) lw[i] = 0xffffffffu;
+      int Ls[kOutLevels];
+      uint64_t Ms[kOutLevels];
+      int nl = 0;
+      uint64_t gtodo = 0, rest = 0;
+      int last = 1;
+#pragma unroll
+      for (int k = 0; k < kOutLevels; ++k) {
+        Ls[k] = 1;
+        Ms[k] = 0;
       }
       if (valid) {
         for (int L0 = 0; L0 < rounds; L0 += kPre) {
@@ -725,10 +648,6 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
               const int b = __ffsll((long long)m) - 1;
               m &= m - 1;
               my_lvl[b] = (uint8_t)L;
-              if (L == 0)
-                my_par[b] = (int32_t)v;
-              else if (L == 1)
-                my_par[b] = p.roots[64 * h + b];
             }
           }
         }
@@ -766,13 +685,14 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
       __syncwarp();
       // rows: lane l of this half, vertices tile*32 .. tile*32 + 31
       const int lanes = min(64, p.k - 64 * h);
-#pragma unroll 8
+#pragma unroll 4
       for (int l = 0; l < lanes; ++l) {
-        const uint8_t lv = lvl[lane * kLvlStride + l];
+        const uint8_t lv = my_lvl[l];
+        const int32_t pv = lv == 0 ? (int32_t)v : (lv == 1 ? p.roots[64 * h + l] : my_par[l]);
         const int64_t at = (int64_t)(64 * h + l) * p.n + v;
         if (valid) {
           p.levels[at] = lv == 0xff ? -1 : (int32_t)lv;
-          p.parents[at] = lv == 0xff ? -1 : par[lane * kParStride + l];
+          p.parents[at] = lv == 0xff ? -1 : pv;
         }
       }
       __syncwarp();
@@ -813,14 +733,6 @@ int ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   CG_CUDA(cudaLaunchKernelEx(&cfg, msbfs_ledger<W>, p));
-  if (s->ncand > 0) {
-    int cand_per_sm = 0;
-    CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cand_per_sm, msbfs_cand_parents<W>,
-                                                          kOutBlock, 0));
-    if (cand_per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
-    msbfs_cand_parents<W><<<cand_per_sm * g->num_sms, kOutBlock, 0, g->stream>>>(p);
-    CG_CUDA(cudaGetLastError());
-  }
   const int smem = kOutWarps * kOutWarpBytes;
   CG_CUDA(cudaFuncSetAttribute(msbfs_outputs<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                smem));
