@@ -31,9 +31,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-# DRAM bytes per launch of bfs_persistent measured with ncu (read + write),
-# scaled per search; see profiles/bfs_persistent_rmat21.md.  None until measured.
-NCU_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) per launch of bfs_persistent, the mean over the 64
+# searches of the default workload measured with ncu (profiles/
+# bfs_persistent_rmat21.md); reported as roofline.traffic for that workload.
+NCU_TRAFFIC_BYTES = {(21, 16, 0, 1): 76.9e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -396,7 +397,7 @@ def run_ours(args):
     step_ms = float(t.item())
   peak, peak_kind = peaks()
   achieved = float(alg_bytes.sum() / (per_root_ms.sum() * 1e-3) / 1e9)
-  traffic = NCU_TRAFFIC_BYTES
+  traffic = NCU_TRAFFIC_BYTES.get((args.scale, args.edgefactor, args.seed, args.root_seed))
   line = {
       "metric": "GTEPS (harmonic mean over 64 roots), per-root direction-optimizing search",
       "value": value * world, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
