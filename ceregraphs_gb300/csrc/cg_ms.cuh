@@ -281,9 +281,43 @@ __device__ __forceinline__ Mask<W> first_holder(const Mask<W> &m) {
 template <int W, bool Ledger>
 __device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, int32_t u,
                                          int32_t v, uint64_t *nxt, uint32_t *touched) {
+  if (Ledger) {
+    // The loads that depend only on v go out together.  A vertex with a
+    // candidate slot takes its parents of this round here: the lowest frontier
+    // source per lane, by atomicMin (after a read, so that hot targets see few
+    // atomics).  The others are found by the output pass's scan of their short
+    // in-lists.
+    const Mask<W> seen = ld_mask<W>(p.vis, v);
+    const Mask<W> have = ld_mask<W>(nxt, v);
+    const int slot = p.cand_slot[v];
+    const uint32_t tw = touched[v >> 5];
+    const Mask<W> f = fu.andnot(seen);
+    if (!f.any()) return false;
+    if (slot >= 0) {
+      uint32_t *cand = p.cand + (int64_t)slot * (64 * W);
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        uint64_t bits = f.w[j];
+        while (bits) {
+          const int b = __ffsll((long long)bits) - 1;
+          bits &= bits - 1;
+          if ((unsigned)u < cand[j * 64 + b]) atomicMin(cand + j * 64 + b, (unsigned)u);
+        }
+      }
+    }
+    const Mask<W> add = f.andnot(have);
+#pragma unroll
+    for (int i = 0; i < W; ++i)
+      if (add.w[i])
+        atomicOr(reinterpret_cast<unsigned long long *>(nxt + (int64_t)v * W + i),
+                 (unsigned long long)add.w[i]);
+    const uint32_t tb = 1u << (v & 31);
+    if (tw & tb) return false;
+    return (atomicOr(touched + (v >> 5), tb) & tb) == 0;
+  }
   const Mask<W> f = fu.andnot(ld_mask<W>(p.vis, v));
   if (!f.any()) return false;
-  const int h = Ledger ? -1 : p.hub_slot[v];
+  const int h = p.hub_slot[v];
   if (h >= 0) {
     const Mask<W> have = ld_mask<W>(p.hub_found, h);
 #pragma unroll
@@ -300,25 +334,6 @@ __device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, i
                  (unsigned long long)add);
     }
     return false;
-  }
-  if (Ledger) {
-    // a vertex with a candidate slot takes its parents of this round here
-    // (the lowest frontier source per lane, by atomicMin); the others are
-    // found by the output pass's scan of their short in-lists
-    const int slot = p.cand_slot[v];
-    if (slot >= 0) {
-      uint32_t *cand = p.cand + (int64_t)slot * (64 * W);
-#pragma unroll
-      for (int j = 0; j < W; ++j) {
-        uint64_t bits = f.w[j];
-        while (bits) {
-          const int b = __ffsll((long long)bits) - 1;
-          bits &= bits - 1;
-          if ((unsigned)u < *(volatile uint32_t *)(cand + j * 64 + b))
-            atomicMin(cand + j * 64 + b, (unsigned)u);
-        }
-      }
-    }
   }
   const Mask<W> add = f.andnot(ld_mask<W>(nxt, v));
   if (add.any()) {

@@ -38,7 +38,7 @@
 namespace cg {
 namespace {
 
-constexpr int kOutBlock = 256;                 // output pass: 8 warps a block
+constexpr int kOutBlock = 128;                 // output pass: 4 warps a block
 constexpr int kOutWarps = kOutBlock / 32;
 constexpr int kOutLevels = 4;                  // levels resolved per in-list scan
 constexpr int kParStride = 65;                 // shared row strides (bank-conflict free)
@@ -111,6 +111,14 @@ __device__ __forceinline__ Mask<W> or_warp_first(const MsParams &p, int64_t s, i
     }
 #pragma unroll
     for (int k = 0; k < G; ++k) f[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+    {
+      // nothing new among these 4 x 32 entries (the common case late in a
+      // list that some lanes only reach in a later round): one reduction
+      Mask<W> any = Mask<W>::zero();
+#pragma unroll
+      for (int k = 0; k < G; ++k) any = any | f[k];
+      if (!warp_or<W>(any & want).andnot(got).any()) continue;
+    }
 #pragma unroll
     for (int k = 0; k < G; ++k) {
       const Mask<W> fk = (f[k] & want).andnot(got);
@@ -119,11 +127,27 @@ __device__ __forceinline__ Mask<W> or_warp_first(const MsParams &p, int64_t s, i
 #pragma unroll
       for (int j = 0; j < W; ++j) {
         if (!F.w[j]) continue;
+        uint32_t *r = row + 64 * j;
+        if (__popcll(F.w[j]) <= 6) {
+          // few lanes: one ballot each
+          uint64_t bits = F.w[j];
+          while (bits) {
+            const int b = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            const unsigned who = __ballot_sync(kMsFull, (fk.w[j] >> b) & 1ull);
+            if (lane == __ffs(who) - 1) {
+              if (atomic)
+                atomicMin(r + b, (unsigned)u[k]);
+              else
+                r[b] = (uint32_t)u[k];
+            }
+          }
+          continue;
+        }
         const uint32_t lo = warp_transpose32((uint32_t)fk.w[j]);
         const uint32_t hi = warp_transpose32((uint32_t)(fk.w[j] >> 32));
         const int32_t plo = __shfl_sync(kMsFull, u[k], lo ? __ffs(lo) - 1 : 0);
         const int32_t phi = __shfl_sync(kMsFull, u[k], hi ? __ffs(hi) - 1 : 0);
-        uint32_t *r = row + 64 * j;
         if (atomic) {
           if (lo) atomicMin(r + lane, (unsigned)plo);
           if (hi) atomicMin(r + lane + 32, (unsigned)phi);

@@ -137,6 +137,7 @@ class Server:
     import torch
     self.torch = torch
     self.graphs = graphs                      # name -> engine.Graph
+    self.lane_words = lane_words
     self.pools = {k: Pool(g, lane_words) for k, g in graphs.items()}
     self.budget = hbm_budget_bytes
     self.in_use = 0
@@ -217,6 +218,116 @@ class Server:
   def close(self):
     for p in self.pools.values():
       p.close()
+
+
+class BatchServer:
+  """Dynamic batching: whenever a graph has no search in flight, the queries
+  waiting for it start together -- one batched launch (64 or 128 bit lanes,
+  outputs written once after the rounds) when at least ``batch_min`` wait,
+  else one per-root search each (the lower latency at light load).  Queries
+  that arrive meanwhile wait for the graph's next launch.  Launches go to the
+  graphs' own streams but are chained by events, so at most one of these
+  persistent, grid-synchronising kernels runs at a time (two of them sharing
+  the GPU could each wait at a grid-wide barrier for blocks the other one
+  keeps from being scheduled)."""
+
+  def __init__(self, graphs, lane_words=1, hbm_budget_bytes=None, batch_min=4, on_done=None):
+    import torch
+    self.torch = torch
+    self.graphs = graphs
+    self.lanes = 64 * int(lane_words)
+    for g in graphs.values():
+      g.set_options(lane_words=int(lane_words))
+    self.budget = hbm_budget_bytes
+    self.batch_min = batch_min
+    self.on_done = on_done
+    self.in_use = 0
+    self.launches = {"batched": 0, "per_root": 0}
+    self._last = None                       # event of the latest launch, any graph
+
+  def _launch(self, name, qs):
+    torch = self.torch
+    g = self.graphs[name]
+    k = len(qs)
+    lv = torch.empty((k, g.n), dtype=torch.int32, device="cuda")
+    pa = torch.empty((k, g.n), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.ExternalStream(g.stream)
+    # the outputs were allocated on torch's stream: the graph's stream waits for it
+    ready = torch.cuda.Event()
+    ready.record(torch.cuda.current_stream())
+    stream.wait_event(ready)
+    if self._last is not None:
+      stream.wait_event(self._last)
+    if k >= self.batch_min:
+      g.msbfs_device([q.root for q in qs], lv, pa)
+      self.launches["batched"] += 1
+    else:
+      for i, q in enumerate(qs):
+        g.bfs_device(q.root, lv[i], pa[i])
+      self.launches["per_root"] += k
+    done = torch.cuda.Event()
+    done.record(stream)
+    self._last = done
+    for i, q in enumerate(qs):
+      q.levels, q.parents = lv[i], pa[i]
+    return done
+
+  def run(self, arrivals, realtime=True):
+    torch = self.torch
+    torch.cuda.synchronize()
+    waiting = {k: deque() for k in self.graphs}
+    inflight = {}                           # graph -> (queries, event, bytes)
+    todo = deque(Query(i, g, r, t) for i, (t, g, r) in enumerate(arrivals))
+    report = ServeReport()
+    t0 = time.perf_counter()
+    clock = (lambda: time.perf_counter() - t0) if realtime else (lambda: float("inf"))
+    while todo or inflight or any(waiting.values()):
+      now = clock()
+      while todo and todo[0].t_arrival <= now:
+        q = todo.popleft()
+        if not realtime:
+          q.t_arrival = time.perf_counter() - t0
+        waiting[q.graph].append(q)
+      for name, wq in waiting.items():
+        if not wq or name in inflight:
+          continue
+        n = self.graphs[name].n
+        take = min(len(wq), self.lanes)
+        if self.budget is not None:
+          take = min(take, max(0, (self.budget - self.in_use) // (8 * n)))
+        if take == 0:
+          continue
+        qs = [wq.popleft() for _ in range(take)]
+        tnow = time.perf_counter() - t0
+        for q in qs:
+          q.t_admit = tnow
+        nbytes = 8 * n * take
+        self.in_use += nbytes
+        inflight[name] = (qs, self._launch(name, qs), nbytes)
+        report.steps += 1
+      for name in list(inflight):
+        qs, ev, nbytes = inflight[name]
+        if not ev.query():
+          continue
+        tnow = time.perf_counter() - t0
+        for q in qs:
+          q.t_done = tnow
+          if self.on_done is not None:
+            self.on_done(q)
+          q.levels = q.parents = None
+          report.queries.append(q)
+        self.in_use -= nbytes
+        del inflight[name]
+      if not inflight and todo and realtime:
+        wait = todo[0].t_arrival - clock()
+        if wait > 0:
+          time.sleep(min(wait, 0.001))
+    report.wall_s = time.perf_counter() - t0
+    report.queries.sort(key=lambda q: q.qid)
+    return report
+
+  def close(self):
+    pass
 
 
 def serial_baseline(graphs, arrivals, realtime=True, on_done=None):

@@ -149,3 +149,39 @@ def test_server_mix_equals_alone_under_hbm_budget(built_lib):
   assert len(base.queries) == 300
   for g in graphs.values():
     g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batch_min", [1, 4, 1000])
+def test_batch_server_equals_alone(built_lib, batch_min):
+  """Dynamic batching (batched launches for busy graphs, per-root searches for
+  light queues): every query's result equals the same search run alone."""
+  from ceregraphs_gb300.engine import Graph
+  arrays = {"rmat13": generators.rmat(13, 16, 2), "grid": generators.grid2d(60)}
+  graphs = {k: Graph(a) for k, a in arrays.items()}
+  roots = {k: graph500.pick_sources(a, 300, 5) for k, a in arrays.items()}
+  arrivals = serving.poisson_arrivals(50000.0, 400, roots, seed=6)
+  alone = {}
+  for k, g in graphs.items():
+    for r in {r for _, gg, r in arrivals if gg == k}:
+      lv, pa, _ = g.bfs(r)
+      alone[(k, r)] = (lv, pa)
+  checked = []
+
+  def on_done(q):
+    wl, wp = alone[(q.graph, q.root)]
+    checked.append(np.array_equal(q.levels.cpu().numpy(), wl) and
+                   np.array_equal(q.parents.cpu().numpy(), wp))
+
+  budget = 100 * 8 * max(a.n for a in arrays.values())
+  srv = serving.BatchServer(graphs, lane_words=1, hbm_budget_bytes=budget, batch_min=batch_min,
+                            on_done=on_done)
+  rep = srv.run(arrivals, realtime=True)
+  assert len(rep.queries) == 400 and len(checked) == 400 and all(checked)
+  assert srv.in_use == 0
+  if batch_min == 1000:
+    assert srv.launches["batched"] == 0
+  s = rep.summary()
+  assert s["p99_ms"] >= s["p50_ms"] > 0
+  for g in graphs.values():
+    g.close()
