@@ -61,7 +61,7 @@ struct MsParams {
   const int64_t *__restrict__ out_off;
   const int32_t *__restrict__ out_idx;
   uint64_t *vis, *fr0, *fr1, *fr2;
-  uint32_t *touched0, *touched1;
+  uint32_t *touched0, *touched1, *touched2;
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
@@ -202,9 +202,11 @@ __device__ __forceinline__ void acc_lanes(MsAcc &acc, const Mask<W> &m) {
 }
 
 // Appends claimed vertices to a frontier list: light ones at the front of
-// `q`, big ones (out-degree > kLightMax) at the back with the prefix offset of
-// their edge lists (one packed atomic per warp: count << 32 | edges).  All 32
-// lanes call.
+// `q` (unless LightQ is false: the ledger kernel finds them in a claim
+// bitmap), big ones (out-degree > kLightMax) at the back with the prefix
+// offset of their edge lists (one packed atomic per warp: count << 32 |
+// edges).  All 32 lanes call.
+template <bool LightQ = true>
 __device__ __forceinline__ void ms_enqueue(bool claimed, int32_t v, int64_t deg, int32_t *q,
                                            int64_t qcap, uint32_t *boff, unsigned *nlight,
                                            unsigned long long *big, MsAcc &acc) {
@@ -214,7 +216,7 @@ __device__ __forceinline__ void ms_enqueue(bool claimed, int32_t v, int64_t deg,
   const bool heavy = claimed && deg > kLightMax;
   const unsigned below = (1u << lane) - 1u;
   const unsigned ml = __ballot_sync(kMsFull, light);
-  if (ml) {
+  if (LightQ && ml) {
     const int leader = __ffs(ml) - 1;
     unsigned base = 0;
     if (lane == leader) base = atomicAdd(nlight, (unsigned)__popc(ml));
@@ -579,6 +581,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.ncand = s->ncand;
   p.touched0 = s->touched;
   p.touched1 = s->touched + p.words;
+  p.touched2 = s->touched + 2 * p.words;
   p.queue0 = s->queue;
   p.queue1 = s->queue + g->n;
   p.bigoff0 = s->bigoff;

@@ -789,7 +789,7 @@ static int ms_create_state(cg_graph *g, int lane_words, int hist_planes, MsState
   const size_t bits = sizeof(uint64_t) * (1 + (size_t)s->hist_planes) * (size_t)g->n * lane_words;
   const size_t words = (size_t)((g->n + 31) / 32);
   if (cudaMalloc(&s->bits, bits) != cudaSuccess ||
-      cudaMalloc(&s->touched, sizeof(uint32_t) * 2 * words) != cudaSuccess ||
+      cudaMalloc(&s->touched, sizeof(uint32_t) * 3 * words) != cudaSuccess ||
       cudaMalloc(&s->queue, sizeof(int32_t) * 2 * (size_t)g->n) != cudaSuccess ||
       cudaMalloc(&s->bigoff, sizeof(uint32_t) * 2 * (size_t)s->bcap) != cudaSuccess ||
       cudaMalloc(&s->ctl, sizeof(MsCtl)) != cudaSuccess ||
@@ -803,7 +803,7 @@ static int ms_create_state(cg_graph *g, int lane_words, int hist_planes, MsState
     ms_free_state(s);
     return rc;
   }
-  g->device_bytes += bits + sizeof(uint32_t) * 2 * words + sizeof(int32_t) * 2 * g->n +
+  g->device_bytes += bits + sizeof(uint32_t) * 3 * words + sizeof(int32_t) * 2 * g->n +
                      sizeof(uint32_t) * 2 * s->bcap + sizeof(MsCtl);
   *out = s;
   return CG_OK;

@@ -24,8 +24,14 @@
 //
 // Rounds: a pull round ORs the frontier masks of a vertex's in-neighbours
 // until every wanted lane is found; a push round ORs frontier masks into
-// out-neighbours' next masks with atomicOr, then merges them into vis.  Hubs'
-// in-lists are split into chunks across warps as in the direct kernel.
+// out-neighbours' next masks with atomicOr.  Hubs' in-lists are split into
+// chunks across warps as in the direct kernel.  The frontier set of round L is
+// a claim bitmap T_L (one bit per vertex, set by whoever first gives the
+// vertex a lane): push rounds find their light frontier vertices there and
+// only big ones (out-degree > kLightMax) go through a queue, so no per-vertex
+// atomic on a shared queue counter.  vis is merged lazily: round L folds F_L
+// into vis for its frontier vertices and tests "visited" as vis | F_L, so a
+// push round needs no second phase.
 //
 // A search that needs more rounds than the history holds sets a flag and
 // stops; the output pass then only clears the control block, and the direct
@@ -163,6 +169,18 @@ __device__ __forceinline__ Mask<W> or_warp_first(const MsParams &p, int64_t s, i
   return got;
 }
 
+// Claim bitmap T_L: one bit per vertex with a nonzero frontier mask F_L --
+// round L's frontier set.  Round L reads T_L (push rounds enumerate light
+// frontier vertices from it), sets T_{L+1}, and clears T_{L+2}; three rotate.
+__device__ __forceinline__ uint32_t *claims(const MsParams &p, int L) {
+  const int r = L % 3;
+  return r == 0 ? p.touched0 : (r == 1 ? p.touched1 : p.touched2);
+}
+
+// vis is merged lazily: a vertex's frontier lanes F_L[v] join vis[v] during
+// round L (pull rounds for every vertex, push rounds for every frontier
+// vertex), so round L tests "visited" as vis | F_L.
+
 // Pull round: light vertices one thread each, medium vertices one warp each,
 // hub in-lists by chunks (ORed into hub_found, merged after the wait).
 template <int W>
@@ -172,14 +190,17 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   const int next_parity = (L + 1) & 1;
   int32_t *q = next_parity ? p.queue1 : p.queue0;
   uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
+  uint32_t *tnext = claims(p, L + 1);
+  const int lane = lane_id();
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
        base < p.n; base += nthreads) {
-    const int64_t v = base + lane_id();
+    const int64_t v = base + lane;
     Mask<W> want = Mask<W>::zero();
-    Mask<W> seen = Mask<W>::zero();
     int64_t s = 0, e = 0;
     if (v < p.n) {
-      seen = ld_mask<W>(p.vis, v);
+      const Mask<W> fv = ld_mask<W>(cur, v);
+      const Mask<W> seen = ld_mask<W>(p.vis, v) | fv;
+      if (fv.any()) st_mask<W>(p.vis, v, seen);
       want = active.andnot(seen);
       if (want.any()) {
         s = __ldg(p.in_off + v);
@@ -190,37 +211,34 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     if (!__ballot_sync(kMsFull, want.any())) continue;
     Mask<W> got = Mask<W>::zero();
     if (want.any()) got = or_thread<W>(p, s, e, want, cur);
-    bool claimed = false;
+    const bool claimed = got.any();
     int64_t deg = 0;
-    if (got.any()) {
+    if (claimed) {
       st_mask<W>(nxt, v, got);
-      st_mask<W>(p.vis, v, seen | got);
-      claimed = true;
-      acc.visits += (unsigned long long)got.popc();
       acc_lanes<W>(acc, got);
       deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
     }
-    ms_enqueue(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+    const unsigned cm = __ballot_sync(kMsFull, claimed);
+    if (lane == 0 && cm) atomicOr(tnext + (base >> 5), cm);
+    ms_enqueue<false>(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
   const int nwarps = (int)(nthreads >> 5);
   for (int64_t j = warp_id_global(); j < p.nmed; j += nwarps) {
     const int32_t v = p.med_vtx[j];
-    const Mask<W> seen = ld_mask<W>(p.vis, v);
-    const Mask<W> want = active.andnot(seen);
+    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
     if (!want.any()) continue;
     // medium vertex j has candidate slot j: its parents of this round go there
     const Mask<W> got = or_warp_first<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1), want,
                                          cur, p.cand + j * (64 * W), false);
-    const bool claimed = lane_id() == 0 && got.any();
+    const bool claimed = lane == 0 && got.any();
     int64_t deg = 0;
     if (claimed) {
       st_mask<W>(nxt, v, got);
-      st_mask<W>(p.vis, v, seen | got);
-      acc.visits += (unsigned long long)got.popc();
+      atomicOr(tnext + (v >> 5), 1u << (v & 31));
       acc_lanes<W>(acc, got);
       deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
     }
-    ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+    ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
   if (p.nhub == 0) return;
   const unsigned nchunks = p.hub_choff[p.nhub];
@@ -235,14 +253,14 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     }
     const int h = (int)lo;
     const int32_t v = p.hub_vtx[h];
-    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v));
+    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
     if (!want.any()) continue;
     const int64_t s = __ldg(p.in_off + v) + (int64_t)(c - p.hub_choff[h]) * kHubChunk;
     const int64_t e = min(s + (int64_t)kHubChunk, __ldg(p.in_off + v + 1));
     // hub h has candidate slot nmed + h; several warps scan its chunks
     const Mask<W> got = or_warp_first<W>(p, s, e, want, cur,
                                          p.cand + (p.nmed + h) * (64 * W), true);
-    if (lane_id() == 0) {
+    if (lane == 0) {
 #pragma unroll
       for (int j = 0; j < W; ++j)
         if (got.w[j])
@@ -253,7 +271,7 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
 }
 
 // After the wait that ends a pull round's scans: hubs found this round get
-// their next mask and vis, and are queued after the round's other vertices.
+// their next mask and claim bit, and are queued if big.
 template <int W>
 __device__ void lg_hub_merge(const MsParams &p, int L, uint64_t *nxt, MsRound *Rn, MsAcc &acc) {
   const int lane = lane_id();
@@ -261,6 +279,7 @@ __device__ void lg_hub_merge(const MsParams &p, int L, uint64_t *nxt, MsRound *R
   const int next_parity = (L + 1) & 1;
   int32_t *q = next_parity ? p.queue1 : p.queue0;
   uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
+  uint32_t *tnext = claims(p, L + 1);
   for (int64_t h0 = (int64_t)warp_id_global() * 32; h0 < p.nhub; h0 += (int64_t)nwarps * 32) {
     const int64_t h = h0 + lane;
     bool claimed = false;
@@ -271,59 +290,258 @@ __device__ void lg_hub_merge(const MsParams &p, int L, uint64_t *nxt, MsRound *R
       if (found.any()) {
         v = p.hub_vtx[h];
         st_mask<W>(nxt, v, found);
-        st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | found);
         st_mask<W>(p.hub_found, h, Mask<W>::zero());
-        acc.visits += (unsigned long long)found.popc();
+        atomicOr(tnext + (v >> 5), 1u << (v & 31));
         acc_lanes<W>(acc, found);
         deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
         claimed = true;
       }
     }
-    ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+    ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
 }
 
-// After a push round: the vertices it queued merge their new lanes into vis.
+// Edge u -> v of a push round: the lanes of u's frontier that v has neither
+// visited nor in its own frontier of this round are ORed into v's next mask
+// (after a read, so hot targets see few atomics); a vertex with a candidate
+// slot also takes u as a parent candidate per lane (atomicMin).  The loads
+// that depend only on v go out together.  Returns whether this thread
+// claimed v (set its bit in the next claim bitmap first).
 template <int W>
-__device__ void lg_push_merge(const MsParams &p, int L, const uint64_t *nxt, MsRound *Rn,
-                              MsAcc &acc) {
-  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  const int next_parity = (L + 1) & 1;
-  const int32_t *q = next_parity ? p.queue1 : p.queue0;
-  const int64_t nl = *(volatile unsigned *)&Rn->res_light;
-  const int64_t nbg = *(volatile unsigned *)&Rn->res_big;
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nl + nbg; j += nthreads) {
-    const int64_t v = j < nl ? q[j] : q[p.n - 1 - (j - nl)];
-    const Mask<W> nw = ld_mask<W>(nxt, v);
-    st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | nw);
-    acc.visits += (unsigned long long)nw.popc();
-    acc_lanes<W>(acc, nw);
+__device__ __forceinline__ bool lg_relax(const MsParams &p, const Mask<W> &fu, int32_t u,
+                                         int32_t v, const uint64_t *cur, uint64_t *nxt,
+                                         uint32_t *tnext, MsAcc &acc) {
+  const Mask<W> seen = ld_mask<W>(p.vis, v);
+  const Mask<W> now = ld_mask<W>(cur, v);
+  const Mask<W> have = ld_mask<W>(nxt, v);
+  const int slot = p.cand_slot[v];
+  const uint32_t tw = tnext[v >> 5];
+  const Mask<W> f = fu.andnot(seen | now);
+  if (!f.any()) return false;
+  acc_lanes<W>(acc, f);
+  if (slot >= 0) {
+    uint32_t *cand = p.cand + (int64_t)slot * (64 * W);
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      uint64_t bits = f.w[j];
+      while (bits) {
+        const int b = __ffsll((long long)bits) - 1;
+        bits &= bits - 1;
+        if ((unsigned)u < cand[j * 64 + b]) atomicMin(cand + j * 64 + b, (unsigned)u);
+      }
+    }
+  }
+  const Mask<W> add = f.andnot(have);
+#pragma unroll
+  for (int i = 0; i < W; ++i)
+    if (add.w[i])
+      atomicOr(reinterpret_cast<unsigned long long *>(nxt + (int64_t)v * W + i),
+               (unsigned long long)add.w[i]);
+  const uint32_t tb = 1u << (v & 31);
+  if (tw & tb) return false;
+  return (atomicOr(tnext + (v >> 5), tb) & tb) == 0;
+}
+
+template <int W>
+__device__ __forceinline__ void lg_step(const MsParams &p, bool valid, const Mask<W> &fu,
+                                        int32_t u, int64_t e, const uint64_t *cur, uint64_t *nxt,
+                                        uint32_t *tnext, int32_t *q, uint32_t *boff, MsRound *Rn,
+                                        MsAcc &acc) {
+  bool claimed = false;
+  int32_t v = 0;
+  int64_t deg = 0;
+  if (valid) {
+    v = __ldg(p.out_idx + e);
+    claimed = lg_relax<W>(p, fu, u, v, cur, nxt, tnext, acc);
+    if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+  }
+  ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+}
+
+// Edge positions [x0, x1) of the big-vertex edge space (queue entries
+// q[cap-1-j] with prefix offsets boff[j], all of out-degree > kLightMax).
+template <int W>
+__device__ void lg_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *nxt,
+                              uint32_t *tnext, const int32_t *bq, const uint32_t *boff,
+                              unsigned nbig, unsigned x0, unsigned x1, int32_t *q, uint32_t *qoff,
+                              MsRound *Rn, MsAcc &acc) {
+  const int lane = lane_id();
+  const int64_t cap = p.n;
+  unsigned lo = 0, hi = nbig - 1;
+  while (lo < hi) {
+    const unsigned mid = (lo + hi + 1) >> 1;
+    if (boff[mid] <= x0)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  unsigned j = lo;
+  int32_t vj = bq[cap - 1 - (int64_t)j];
+  int64_t sj = __ldg(p.out_off + vj);
+  unsigned oj = boff[j];
+  unsigned endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
+  Mask<W> fj = ld_mask<W>(cur, vj);
+  for (unsigned base = x0; base < x1; base += 32) {
+    while (base >= endj) {
+      ++j;
+      vj = bq[cap - 1 - (int64_t)j];
+      sj = __ldg(p.out_off + vj);
+      oj = boff[j];
+      endj = oj + (unsigned)(__ldg(p.out_off + vj + 1) - sj);
+      fj = ld_mask<W>(cur, vj);
+    }
+    const unsigned x = base + lane;
+    const bool valid = x < x1;
+    int32_t u = vj;
+    int64_t e = sj + (int64_t)(x - oj);
+    Mask<W> fu = fj;
+    if (__ballot_sync(kMsFull, valid && x >= endj)) {
+      const int32_t vn = bq[cap - 1 - (int64_t)(j + 1)];
+      if (valid && x >= endj) {
+        u = vn;
+        e = __ldg(p.out_off + vn) + (int64_t)(x - endj);
+        fu = ld_mask<W>(cur, vn);
+      }
+    }
+    lg_step<W>(p, valid, fu, u, e, cur, nxt, tnext, q, qoff, Rn, acc);
   }
 }
 
-// End of round L (last block to arrive): as the direct kernel's, plus the
-// history bound -- round L + 1 writes F_{L+2}, which must be a plane.
+// Push round.  Work items: the big vertices' edges in chunks (from the
+// queue, as in the direct kernel), then groups of 32 claim words (1024
+// vertices): the frontier vertices there merge their lanes into vis, and the
+// light ones (out-degree <= kLightMax) spread their edges over the warp.
+template <int W>
+__device__ void lg_push(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
+                        MsRound *Rc, MsRound *Rn, MsAcc &acc) {
+  __shared__ int32_t s_u[kMsBlock / 32][32];
+  __shared__ int64_t s_s[kMsBlock / 32][32];
+  __shared__ int64_t s_x[kMsBlock / 32][32];
+  const int lane = lane_id();
+  const int wib = threadIdx.x >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int parity = L & 1, next_parity = parity ^ 1;
+  const int32_t *qc = parity ? p.queue1 : p.queue0;
+  const uint32_t *bc = parity ? p.bigoff1 : p.bigoff0;
+  int32_t *qn = next_parity ? p.queue1 : p.queue0;
+  uint32_t *bn = next_parity ? p.bigoff1 : p.bigoff0;
+  const uint32_t *tcur = claims(p, L);
+  uint32_t *tnext = claims(p, L + 1);
+
+  const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
+  const unsigned nbig = (unsigned)(bigw >> 32), big_edges = (unsigned)bigw;
+  unsigned chunk = ((big_edges / (unsigned)nwarps) + 31u) & ~31u;
+  chunk = chunk < 32u ? 32u : (chunk > (unsigned)kPushChunk ? (unsigned)kPushChunk : chunk);
+  const unsigned nb = (big_edges + chunk - 1) / chunk;
+  const unsigned ngroups = (unsigned)((p.words + 31) / 32);
+  const unsigned nitems = nb + ngroups;
+  unsigned item = (unsigned)warp_id_global();
+  while (item < nitems) {
+    if (item < nb) {
+      const unsigned x0 = item * chunk;
+      lg_push_chunk<W>(p, cur, nxt, tnext, qc, bc, nbig, x0, min(x0 + chunk, big_edges), qn, bn,
+                       Rn, acc);
+    } else {
+      // the group's frontier vertices, compacted 32 at a time: lane j holds
+      // word j; the t-th frontier vertex is the (t - prefix)-th set bit of the
+      // word whose prefix count covers t
+      const int64_t w0 = (int64_t)(item - nb) * 32;
+      const uint32_t mine = w0 + lane < p.words ? tcur[w0 + lane] : 0u;
+      const int cnt = __popc(mine);
+      int incl_c = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kMsFull, incl_c, o);
+        if (lane >= o) incl_c += t;
+      }
+      const int total_v = __shfl_sync(kMsFull, incl_c, 31);
+      for (int b0 = 0; b0 < total_v; b0 += 32) {
+        const int t = b0 + lane;
+        int32_t u = -1;
+        int64_t s = 0, d = 0;
+        // word holding the t-th vertex: the first lane whose inclusive count
+        // exceeds t (the counts never decrease)
+        int wsel = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (__shfl_sync(kMsFull, incl_c, wsel + step - 1) <= t) wsel += step;
+        const uint32_t wbits = __shfl_sync(kMsFull, mine, wsel);
+        const int before = __shfl_sync(kMsFull, incl_c - cnt, wsel);
+        if (t < total_v) {
+          const int bit = __fns(wbits, 0, t - before + 1);
+          const int64_t v = (w0 + wsel) * 32 + bit;
+          const Mask<W> fv = ld_mask<W>(cur, v);
+          st_mask<W>(p.vis, v, ld_mask<W>(p.vis, v) | fv);
+          s = __ldg(p.out_off + v);
+          d = __ldg(p.out_off + v + 1) - s;
+          if (d > kLightMax)
+            d = 0;  // big: its edges are in the chunks above
+          else
+            u = (int32_t)v;
+        }
+        int64_t incl = d;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int64_t tt = __shfl_up_sync(kMsFull, incl, o);
+          if (lane >= o) incl += tt;
+        }
+        const int64_t total = __shfl_sync(kMsFull, incl, 31);
+        s_u[wib][lane] = u;
+        s_s[wib][lane] = s;
+        s_x[wib][lane] = incl - d;
+        __syncwarp();
+        for (int64_t base = 0; base < total; base += 32) {
+          const int64_t t2 = base + lane;
+          const bool valid = t2 < total;
+          int64_t e = 0;
+          int32_t uu = 0;
+          Mask<W> fu = Mask<W>::zero();
+          if (valid) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (s_x[wib][mid] <= t2)
+                lo = mid;
+              else
+                hi = mid - 1;
+            }
+            uu = s_u[wib][lo];
+            fu = ld_mask<W>(cur, uu);
+            e = s_s[wib][lo] + (t2 - s_x[wib][lo]);
+          }
+          lg_step<W>(p, valid, fu, uu, e, cur, nxt, tnext, qn, bn, Rn, acc);
+        }
+        __syncwarp();
+      }
+    }
+    unsigned nextitem = 0;
+    if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
+    item = __shfl_sync(kMsFull, nextitem, 0);
+  }
+}
+
+// End of round L (last block to arrive): termination, the next direction,
+// statistics, the history bound -- round L + 1 writes F_{L+2}, which must be
+// a plane -- and the reset of the record round L + 1 fills.  Lane discoveries
+// per round are counted by the output pass, from the history.
 template <int W>
 __device__ unsigned lg_decide(const MsParams &p, int L, int dir, int ran) {
   MsCtl *ctl = p.ctl;
   const MsRound *Rn = &ctl->rec[(L + 1) % kRing];
-  unsigned long long nf = 0, visits = 0, mf = 0;
+  unsigned long long nf = 0, mf = 0;
 #pragma unroll
   for (int i = 0; i < kCounterShards; ++i) {
     nf += *(volatile const unsigned long long *)&Rn->nf[i];
-    visits += *(volatile const unsigned long long *)&Rn->visits[i];
     mf += *(volatile const unsigned long long *)&Rn->mf[i];
   }
   cg_stats *st = p.stats;
   const long long now = global_ns();
   if (ran < CG_HISTORY) {
-    st->nf_history[ran] = (int64_t)visits;
     st->direction_history[ran] = dir;
     st->round_ns[ran] = now - ctl->t_round;
   }
   ctl->t_round = now;
   if (dir == 1) ctl->pull_rounds += 1;
-  ctl->visited += visits;
   bool stop = nf == 0;
   if (!stop && L + 1 >= p.level_cap) {
     atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
@@ -353,7 +571,6 @@ __device__ unsigned lg_decide(const MsParams &p, int L, int dir, int ran) {
     const int rounds = ran + 1;
     st->status = *(volatile int *)&ctl->status;
     st->rounds = rounds;
-    st->visited = (int64_t)ctl->visited;
     st->pull_rounds = ctl->pull_rounds;
     st->switches = ctl->switches;
     st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
@@ -369,15 +586,6 @@ struct LgRoundDecision {
   __device__ unsigned operator()() const { return lg_decide<W>(*p, L, dir, ran); }
 };
 
-struct LgResolveSnapshot {
-  MsRound *R;
-  __device__ unsigned operator()() const {
-    R->res_light = *(volatile unsigned *)&R->nlight;
-    R->res_big = (unsigned)(*(volatile unsigned long long *)&R->big >> 32);
-    return 0u;
-  }
-};
-
 struct LgSetupDecision {
   MsCtl *ctl;
   cg_stats *st;
@@ -385,13 +593,16 @@ struct LgSetupDecision {
     const long long now = global_ns();
     st->setup_ns = now - ctl->t_start;
     st->finish_ns = 0;
+    st->visited = 0;
+    for (int i = 0; i < CG_HISTORY; ++i) st->nf_history[i] = 0;
     ctl->t_round = now;
     return 0u;
   }
 };
 
 // The rounds of one batch (cooperative, persistent): roots[0..k) seeded in
-// F_0; round L reads F_L, writes F_{L+1} and clears F_{L+2}.
+// F_0 and T_0; round L reads F_L and T_L, writes F_{L+1} and T_{L+1}, clears
+// F_{L+2} and T_{L+2}.
 template <int W>
 __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
   __shared__ unsigned s_payload;
@@ -408,22 +619,21 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
   for (int64_t w = gtid; w < p.words; w += nthreads) {
     p.touched0[w] = 0;
     p.touched1[w] = 0;
+    p.touched2[w] = 0;
   }
   bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
   if (ok && blockIdx.x == 0 && threadIdx.x < p.k) {
     const int i = threadIdx.x;
     const int32_t r = p.roots[i];
     const unsigned long long bit = 1ull << (i & 63);
-    atomicOr(reinterpret_cast<unsigned long long *>(p.vis + (int64_t)r * W + (i >> 6)), bit);
     atomicOr(reinterpret_cast<unsigned long long *>(f0 + (int64_t)r * W + (i >> 6)), bit);
+    atomicOr(p.touched0 + (r >> 5), 1u << (r & 31));
     bool first = true;
     for (int j = 0; j < i; ++j) first = first && (p.roots[j] != r);
     if (first) {
       const int64_t deg = p.out_off[r + 1] - p.out_off[r];
       MsRound *R0 = &ctl->rec[0];
-      if (deg <= kLightMax) {
-        p.queue0[atomicAdd(&R0->nlight, 1u)] = r;
-      } else {
+      if (deg > kLightMax) {
         const unsigned long long old = atomicAdd(&R0->big, (1ull << 32) | (unsigned long long)deg);
         p.queue0[p.n - 1 - (int64_t)(old >> 32)] = r;
         p.bigoff0[old >> 32] = (unsigned)old;
@@ -435,7 +645,6 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
       const Mask<W> a0 = lane_mask<W>(p.k);
       ctl->rec[0].lanes[0] = a0.w[0];
       ctl->rec[0].lanes[1] = W == 2 ? a0.w[W - 1] : 0ull;
-      ctl->visited = (unsigned long long)p.k;
     }
   }
   if (ok) {
@@ -451,15 +660,14 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
   while (ok) {
     const uint64_t *cur = plane<W>(p, L);
     uint64_t *nxt = plane<W>(p, L + 1);
-    uint32_t *touched = (L & 1) ? p.touched1 : p.touched0;
-    uint32_t *touched_next = (L & 1) ? p.touched0 : p.touched1;
     MsRound *Rc = &ctl->rec[L % kRing];
     MsRound *Rn = &ctl->rec[(L + 1) % kRing];
     if (L + 2 < p.hist_planes) {
       uint64_t *clr = plane<W>(p, L + 2);
       for (int64_t i = gtid; i < p.n * W; i += nthreads) clr[i] = 0;
     }
-    for (int64_t w = gtid; w < p.words; w += nthreads) touched_next[w] = 0;
+    uint32_t *tclr = claims(p, L + 2);
+    for (int64_t w = gtid; w < p.words; w += nthreads) tclr[w] = 0;
     if (dir == 1) {
       Mask<W> active;
 #pragma unroll
@@ -470,23 +678,12 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
         lg_hub_merge<W>(p, L, nxt, Rn, acc);
       }
     } else {
-      ms_push<W, true>(p, L, cur, nxt, touched, Rc, Rn, acc);
-      __syncthreads();
-      if (threadIdx.x == 0)
-        s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
-                                    LgResolveSnapshot{Rn});
-      __syncthreads();
-      if (s_payload == kWaitFailed) {
-        ok = false;
-        break;
-      }
-      lg_push_merge<W>(p, L, nxt, Rn, acc);
+      lg_push<W>(p, L, cur, nxt, Rc, Rn, acc);
     }
     ms_block_totals(acc, tot);
     if (threadIdx.x == 0) {
       const int sh = blockIdx.x % kCounterShards;
       if (tot.nf) atomicAdd(&Rn->nf[sh], tot.nf);
-      if (tot.visits) atomicAdd(&Rn->visits[sh], tot.visits);
       if (tot.mf) atomicAdd(&Rn->mf[sh], tot.mf);
       if (tot.lanes[0]) atomicOr(&Rn->lanes[0], tot.lanes[0]);
       if (tot.lanes[1]) atomicOr(&Rn->lanes[1], tot.lanes[1]);
@@ -566,6 +763,7 @@ __device__ __forceinline__ uint64_t parent_hits(const MsParams &p, int32_t u, in
 template <int W>
 __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   extern __shared__ __align__(16) unsigned char s_tile[];
+  __shared__ unsigned long long s_cnt[CG_HISTORY + 1];  // lane discoveries per level
   constexpr int kPre = 8;     // history planes loaded together
   constexpr int kScanG = 8;   // in-list entries loaded together
   MsCtl *ctl = p.ctl;
@@ -580,6 +778,9 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   if (*(volatile int *)&ctl->status != 0) return;  // timed out or over the level cap
   int rounds = *(volatile int *)&ctl->L;           // F_0 .. F_rounds, F_rounds empty
   if (rounds > p.hist_planes) rounds = p.hist_planes;
+  if (rounds > CG_HISTORY + 1) rounds = CG_HISTORY + 1;
+  for (int i = threadIdx.x; i <= CG_HISTORY; i += blockDim.x) s_cnt[i] = 0;
+  __syncthreads();
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
   int32_t *par = reinterpret_cast<int32_t *>(s_tile + wib * kOutWarpBytes);
@@ -653,6 +854,7 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
           for (int j = 0; j < kPre; ++j) {
             uint64_t m = pm[j];
             const int L = L0 + j;
+            if (m) atomicAdd(&s_cnt[L], (unsigned long long)__popcll(m));
             if (m && L >= 2 && slot < 0) {
               if (nl < kOutLevels) {
 #pragma unroll
@@ -722,8 +924,17 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
       __syncwarp();
     }
   }
-  // the last block out records the time since the last round ended
+  // the statistics: lane discoveries per round (level L came from round
+  // L - 1) and in all; the last block out records the time since the last
+  // round ended
   __syncthreads();
+  for (int i = threadIdx.x; i < rounds; i += blockDim.x) {
+    const unsigned long long c = s_cnt[i];
+    if (!c) continue;
+    atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->visited), c);
+    if (i >= 1)
+      atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->nf_history[i - 1]), c);
+  }
   if (threadIdx.x == 0 && atomicAdd(&ctl->exited, 1u) + 1u == gridDim.x)
     p.stats->finish_ns = global_ns() - *(volatile long long *)&ctl->t_round;
 }
