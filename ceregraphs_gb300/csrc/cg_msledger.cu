@@ -879,8 +879,13 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
         }
       }
       // light vertices: the whole in-list (<= kPullLight entries), kScanG
-      // entries' loads in flight, kOutLevels levels per pass
+      // entries' loads in flight, kOutLevels levels per pass.  The lanes of
+      // the first entry that hits (often most of them; all of them for an
+      // in-degree of one) are kept as a mask, not stored one by one.
       int from = last + 1;
+      int32_t u_first = 0;
+      uint64_t m_first = 0;
+      bool first_pass = true;
       while (gtodo) {
         for (int64_t j0 = s; j0 < e && gtodo; j0 += kScanG) {
           int32_t u[kScanG];
@@ -894,6 +899,11 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
           for (int k = 0; k < kScanG; ++k) {
             uint64_t bk = b[k] & gtodo;
             gtodo &= ~bk;
+            if (bk && first_pass && !m_first) {
+              m_first = bk;
+              u_first = u[k];
+              bk = 0;
+            }
             while (bk) {
               const int bit = __ffsll((long long)bk) - 1;
               bk &= bk - 1;
@@ -901,6 +911,7 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
             }
           }
         }
+        first_pass = false;
         gtodo = 0;
         if (rest) {  // more than kOutLevels levels at this vertex
           gtodo = collect_levels<W>(p, v, h, rounds, rest, from, Ls, Ms);
@@ -914,7 +925,10 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
 #pragma unroll 4
       for (int l = 0; l < lanes; ++l) {
         const uint8_t lv = my_lvl[l];
-        const int32_t pv = lv == 0 ? (int32_t)v : (lv == 1 ? p.roots[64 * h + l] : my_par[l]);
+        const int32_t pv = lv == 0   ? (int32_t)v
+                         : lv == 1   ? p.roots[64 * h + l]
+                         : ((m_first >> l) & 1ull) ? u_first
+                                                   : my_par[l];
         const int64_t at = (int64_t)(64 * h + l) * p.n + v;
         if (valid) {
           p.levels[at] = lv == 0xff ? -1 : (int32_t)lv;
