@@ -9,7 +9,8 @@
 #include "cg_internal.cuh"
 
 namespace cg {
-int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents);
+int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents,
+               int32_t *host_levels = nullptr, int32_t *host_parents = nullptr);
 int count_edges_launch(cg_graph *g, const int32_t *d_levels, int32_t k, unsigned long long *d_m);
 int msbfs_launch(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels,
                  int32_t *d_parents);
@@ -43,6 +44,7 @@ static void free_graph(cg_graph *g) {
   cudaFree(g->tmp_parents);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
+  if (g->h_stats) cudaFreeHost(g->h_stats);
   if (g->stream) cudaStreamDestroy(g->stream);
   cudaSetDevice(prev);
   delete g;
@@ -222,6 +224,19 @@ int cg_graph_last_stats(cg_graph *g, cg_stats *stats) {
   return CG_OK;
 }
 
+// Device-visible address of a page-locked host buffer, or NULL for pageable
+// memory (which is then filled by an ordinary copy).
+static int32_t *pinned_device_ptr(int32_t *host) {
+  if (!host) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // not a CUDA pointer: clear the sticky-free error
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return static_cast<int32_t *>(a.devicePointer);
+}
+
 int cg_bfs(cg_graph *g, int64_t root, int32_t *levels, int32_t *parents, cg_stats *stats) {
   if (!g || root < 0 || root >= g->n) return CG_ERR_INVALID_ARG;
   if (!g->tmp_levels) {
@@ -231,18 +246,28 @@ int cg_bfs(cg_graph *g, int64_t root, int32_t *levels, int32_t *parents, cg_stat
       return CG_ERR_OUT_OF_MEMORY;
     g->device_bytes += 2 * sizeof(int32_t) * g->n;
   }
+  if (!g->h_stats) {
+    void *h = nullptr;
+    if (cudaHostAlloc(&h, sizeof(cg_stats), cudaHostAllocDefault) != cudaSuccess)
+      return CG_ERR_OUT_OF_MEMORY;
+    g->h_stats = static_cast<cg_stats *>(h);
+  }
+  // page-locked outputs are written by the search kernel itself at its end
+  // (the GPU's own SMs over the host link); pageable ones by a copy after it
+  int32_t *hl = pinned_device_ptr(levels), *hp = pinned_device_ptr(parents);
   CG_CUDA(cudaEventRecord(g->ev0, g->stream));
-  int rc = bfs_launch(g, root, g->tmp_levels, g->tmp_parents);
+  int rc = bfs_launch(g, root, g->tmp_levels, g->tmp_parents, hl, hp);
   if (rc) return rc;
   CG_CUDA(cudaEventRecord(g->ev1, g->stream));
   const size_t bytes = sizeof(int32_t) * (size_t)g->n;
-  if (levels)
+  if (levels && !hl)
     CG_CUDA(cudaMemcpyAsync(levels, g->tmp_levels, bytes, cudaMemcpyDeviceToHost, g->stream));
-  if (parents)
+  if (parents && !hp)
     CG_CUDA(cudaMemcpyAsync(parents, g->tmp_parents, bytes, cudaMemcpyDeviceToHost, g->stream));
-  cg_stats local;
-  CG_CUDA(cudaMemcpyAsync(&local, g->d_stats, sizeof(cg_stats), cudaMemcpyDeviceToHost, g->stream));
+  CG_CUDA(cudaMemcpyAsync(g->h_stats, g->d_stats, sizeof(cg_stats), cudaMemcpyDeviceToHost,
+                          g->stream));
   CG_CUDA(cudaStreamSynchronize(g->stream));
+  cg_stats local = *g->h_stats;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, g->ev0, g->ev1);
   local.device_ms = ms;

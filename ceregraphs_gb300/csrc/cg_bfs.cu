@@ -461,6 +461,26 @@ struct SetupDecision {
   }
 };
 
+// A host caller's outputs, copied by every block into the page-locked
+// buffers (16 bytes a thread when n allows).  Kept out of line so the search
+// loop's registers are not shared with it.
+__device__ __noinline__ void copy_to_host(const BfsParams &p) {
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int a = 0; a < 2; ++a) {
+    const int32_t *src = a ? p.parents : p.levels;
+    int32_t *dst = a ? p.host_parents : p.host_levels;
+    if (!dst) continue;
+    if ((p.n & 3) == 0) {
+      const int4 *s4 = reinterpret_cast<const int4 *>(src);
+      int4 *d4 = reinterpret_cast<int4 *>(dst);
+      for (int64_t i = t0; i < (p.n >> 2); i += step) d4[i] = s4[i];
+    } else {
+      for (int64_t i = t0; i < p.n; i += step) dst[i] = src[i];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
   __shared__ unsigned s_payload;
   BfsCtl *ctl = p.ctl;
@@ -554,6 +574,8 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
     ++L;
   }
   if (leader && s_payload == kWaitFailed) p.stats->status = *(volatile int *)&ctl->status;
+  // after the last wait every output is final
+  if (s_payload != kWaitFailed && (p.host_levels || p.host_parents)) copy_to_host(p);
 }
 
 // Graph500 m per search (bfs_timing.py:379-398), lane = blockIdx.y.
@@ -626,7 +648,8 @@ static int bfs_grid(cg_graph *g) {
   return CG_OK;
 }
 
-int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents) {
+int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents,
+               int32_t *host_levels, int32_t *host_parents) {
   int rc = bfs_prepare(g);
   if (rc) return rc;
   if ((rc = bfs_grid(g))) return rc;
@@ -648,6 +671,8 @@ int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents)
   p.bigoff1 = g->bigoff + g->bcap;
   p.levels = d_levels;
   p.parents = d_parents;
+  p.host_levels = host_levels;
+  p.host_parents = host_parents;
   p.ctl = g->ctl;
   p.stats = g->d_stats;
   p.root = root;

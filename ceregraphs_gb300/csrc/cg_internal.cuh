@@ -93,6 +93,9 @@ struct BfsParams {
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   int32_t *levels, *parents;
+  // page-locked host buffers the finished search is copied into by the
+  // kernel itself (device-visible addresses; NULL = none)
+  int32_t *host_levels, *host_parents;
   BfsCtl *ctl;
   cg_stats *stats;
   int64_t root;
@@ -138,6 +141,7 @@ struct cg_graph {
   int ms_grid = 0, ms_block = 0;
   int64_t device_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cg_stats *h_stats = nullptr;     // page-locked copy target of d_stats
 };
 
 namespace cg {

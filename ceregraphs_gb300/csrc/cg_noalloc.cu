@@ -121,6 +121,8 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   p.bigoff0 = bigoff;
   p.bigoff1 = bigoff + kNoAllocMaxBig;
   p.levels = d_levels;
+  p.host_levels = nullptr;
+  p.host_parents = nullptr;
   p.parents = d_parents;
   p.ctl = reinterpret_cast<BfsCtl *>(base + kOffCtl);
   p.stats = reinterpret_cast<cg_stats *>(base + kOffStats);
