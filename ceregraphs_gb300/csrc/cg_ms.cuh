@@ -15,6 +15,7 @@ constexpr int kMsMaxLanes = 128;
 constexpr int kPullLight = 32;    // in-degree <= this: one thread scans the in-list
 constexpr int kHubDeg = 1024;     // in-degree > this: hub
 constexpr int kHubChunk = 1024;   // in-list entries of a hub per work item
+constexpr int kPairs = 4;         // first-hit records per light vertex (ledger batches)
 
 struct MsRound {
   unsigned long long nf[kCounterShards];      // vertices with a nonzero frontier mask
@@ -95,6 +96,11 @@ struct MsParams {
   const uint32_t *cand_choff; // [ncand + 1] prefix of in-list chunks
   uint32_t *cand;             // [ncand][64 W], 0xFFFFFFFF = none yet
   int ncand;
+  // first hits of light vertices' pull-round scans: up to kPairs (source,
+  // lanes) records per vertex, record q at [q * n + v]
+  int32_t *pair_u;
+  uint64_t *pair_m;           // W words per record
+  uint8_t *pair_n;            // [n] records used
   int gate;                   // run only if *flag is set (the fallback launch)
   int32_t roots[kMsMaxLanes];
 };
@@ -547,6 +553,9 @@ struct MsState {
   uint32_t *cand_choff = nullptr;
   uint32_t *cand = nullptr;
   int ncand = 0;
+  int32_t *pair_u = nullptr;
+  uint64_t *pair_m = nullptr;
+  uint8_t *pair_n = nullptr;
   int64_t bcap = 0;
   int nhub = 0;
   int lane_words = 0;
@@ -579,6 +588,9 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.cand_choff = s->cand_choff;
   p.cand = s->cand;
   p.ncand = s->ncand;
+  p.pair_u = s->pair_u;
+  p.pair_m = s->pair_m;
+  p.pair_n = s->pair_n;
   p.touched0 = s->touched;
   p.touched1 = s->touched + p.words;
   p.touched2 = s->touched + 2 * p.words;

@@ -648,6 +648,9 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->cand_vtx);
   cudaFree(s->cand_choff);
   cudaFree(s->cand);
+  cudaFree(s->pair_u);
+  cudaFree(s->pair_m);
+  cudaFree(s->pair_n);
   delete s;
 }
 
@@ -741,8 +744,13 @@ static int ms_build_cands(cg_graph *g, MsState *s) {
   if (cudaMalloc(&s->cand_slot, sizeof(int32_t) * (size_t)g->n) != cudaSuccess ||
       cudaMalloc(&s->cand_vtx, sizeof(int32_t) * nc) != cudaSuccess ||
       cudaMalloc(&s->cand_choff, sizeof(uint32_t) * (nc + 1)) != cudaSuccess ||
-      cudaMalloc(&s->cand, sizeof(uint32_t) * nc * 64 * s->lane_words) != cudaSuccess)
+      cudaMalloc(&s->cand, sizeof(uint32_t) * nc * 64 * s->lane_words) != cudaSuccess ||
+      cudaMalloc(&s->pair_u, sizeof(int32_t) * kPairs * (size_t)g->n) != cudaSuccess ||
+      cudaMalloc(&s->pair_m, sizeof(uint64_t) * kPairs * (size_t)g->n * s->lane_words) !=
+          cudaSuccess ||
+      cudaMalloc(&s->pair_n, (size_t)((g->n + 3) / 4) * 4) != cudaSuccess)
     return CG_ERR_OUT_OF_MEMORY;
+  g->device_bytes += (sizeof(int32_t) + sizeof(uint64_t) * s->lane_words) * kPairs * g->n + g->n;
   CG_CUDA(cudaMemsetAsync(s->cand_slot, 0xff, sizeof(int32_t) * (size_t)g->n, g->stream));
   if (s->nmed)
     CG_CUDA(cudaMemcpyAsync(s->cand_vtx, s->med_vtx, sizeof(int32_t) * (size_t)s->nmed,

@@ -75,6 +75,44 @@ __device__ __forceinline__ Mask<W> or_thread(const MsParams &p, int64_t s, int64
   return got;
 }
 
+// or_thread that also records, for light vertex v, each in-list entry that
+// brings new lanes -- their lowest-index parent, the scan being ascending --
+// as a (source, lanes) pair, up to kPairs per vertex over all pull rounds.
+// Lanes found after the records run out are left to the output pass's scan.
+template <int W>
+__device__ __forceinline__ Mask<W> or_thread_rec(const MsParams &p, int64_t v, int64_t s,
+                                                 int64_t e, const Mask<W> &want,
+                                                 const uint64_t *cur) {
+  constexpr int G = 4;
+  Mask<W> got = Mask<W>::zero();
+  int used = p.pair_n[v];
+  const int first = used;
+  for (int64_t i0 = s; i0 < e; i0 += G) {
+    int32_t u[G];
+    Mask<W> m[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) u[k] = i0 + k < e ? __ldg(p.in_idx + i0 + k) : -1;
+#pragma unroll
+    for (int k = 0; k < G; ++k) m[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const Mask<W> nb = (m[k] & want).andnot(got);
+      if (nb.any()) {
+        if (used < kPairs) {
+          const int64_t at = (int64_t)used * p.n + v;
+          p.pair_u[at] = u[k];
+          st_mask<W>(p.pair_m, at, nb);
+          ++used;
+        }
+        got = got | nb;
+      }
+    }
+    if (got == want) break;
+  }
+  if (used != first) p.pair_n[v] = (uint8_t)used;
+  return got;
+}
+
 // 32 x 32 bit-matrix transpose across the warp: lane r holds row r (bit c =
 // entry (r, c)); afterwards lane t holds column t (bit r = entry (r, t)).
 // Five butterfly steps, each swapping off-diagonal blocks with the partner
@@ -210,7 +248,7 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     }
     if (!__ballot_sync(kMsFull, want.any())) continue;
     Mask<W> got = Mask<W>::zero();
-    if (want.any()) got = or_thread<W>(p, s, e, want, cur);
+    if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur);
     const bool claimed = got.any();
     int64_t deg = 0;
     if (claimed) {
@@ -621,6 +659,8 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     p.touched1[w] = 0;
     p.touched2[w] = 0;
   }
+  uint32_t *pn = reinterpret_cast<uint32_t *>(p.pair_n);
+  for (int64_t w = gtid; w < (p.n + 3) / 4; w += nthreads) pn[w] = 0;
   bool ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns);
   if (ok && blockIdx.x == 0 && threadIdx.x < p.k) {
     const int i = threadIdx.x;
@@ -844,6 +884,27 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
         Ls[k] = 1;
         Ms[k] = 0;
       }
+      // a light vertex's first-hit records from the pull rounds
+      int32_t pu[kPairs];
+      uint64_t pmk[kPairs];
+      uint64_t covered = 0;
+#pragma unroll
+      for (int q = 0; q < kPairs; ++q) {
+        pu[q] = 0;
+        pmk[q] = 0;
+      }
+      if (valid && slot < 0) {
+        const int np = p.pair_n[v];
+#pragma unroll
+        for (int q = 0; q < kPairs; ++q) {
+          if (q < np) {
+            const int64_t at = (int64_t)q * p.n + v;
+            pu[q] = p.pair_u[at];
+            pmk[q] = p.pair_m[at * W + h];
+            covered |= pmk[q];
+          }
+        }
+      }
       if (valid) {
         for (int L0 = 0; L0 < rounds; L0 += kPre) {
           uint64_t pm[kPre];
@@ -855,19 +916,20 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
             uint64_t m = pm[j];
             const int L = L0 + j;
             if (m) atomicAdd(&s_cnt[L], (unsigned long long)__popcll(m));
-            if (m && L >= 2 && slot < 0) {
+            const uint64_t scan = m & ~covered;
+            if (scan && L >= 2 && slot < 0) {
               if (nl < kOutLevels) {
 #pragma unroll
                 for (int k = 0; k < kOutLevels; ++k)
                   if (k == nl) {
                     Ls[k] = L;
-                    Ms[k] = m;
+                    Ms[k] = scan;
                   }
                 ++nl;
-                gtodo |= m;
+                gtodo |= scan;
                 last = L;
               } else {
-                rest |= m;
+                rest |= scan;
               }
             }
             while (m) {
@@ -925,10 +987,13 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
 #pragma unroll 4
       for (int l = 0; l < lanes; ++l) {
         const uint8_t lv = my_lvl[l];
-        const int32_t pv = lv == 0   ? (int32_t)v
-                         : lv == 1   ? p.roots[64 * h + l]
-                         : ((m_first >> l) & 1ull) ? u_first
-                                                   : my_par[l];
+        int32_t pv = my_par[l];
+        if ((m_first >> l) & 1ull) pv = u_first;
+#pragma unroll
+        for (int q = 0; q < kPairs; ++q)
+          if ((pmk[q] >> l) & 1ull) pv = pu[q];
+        if (lv == 1) pv = p.roots[64 * h + l];
+        if (lv == 0) pv = (int32_t)v;
         const int64_t at = (int64_t)(64 * h + l) * p.n + v;
         if (valid) {
           p.levels[at] = lv == 0xff ? -1 : (int32_t)lv;
