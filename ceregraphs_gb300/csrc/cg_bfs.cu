@@ -400,43 +400,64 @@ constexpr unsigned kDone = 1u, kNextPull = 2u;
 __device__ unsigned decide_round(const BfsParams &p, int L, int dir) {
   BfsCtl *ctl = p.ctl;
   const RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
+  // every load first (from L2: other blocks wrote these), so that they are in
+  // flight together -- this function runs while the whole grid waits
+  unsigned long long nfs[kCounterShards], mfs[kCounterShards], vds[kCounterShards];
+#pragma unroll
+  for (int i = 0; i < kCounterShards; ++i) {
+    nfs[i] = __ldcg(&Rn->nf[i]);
+    mfs[i] = __ldcg(&Rn->mf[i]);
+    vds[i] = __ldcg(&Rn->visdeg[i]);
+  }
+  const long long t_round = __ldcg(&ctl->t_round);
+  const int pull_rounds = __ldcg(&ctl->pull_rounds);
+  const int switches = __ldcg(&ctl->switches);
+  const unsigned long long visited = __ldcg(&ctl->visited);
+  const unsigned long long prev_nf = __ldcg(&ctl->prev_nf);
+  const unsigned long long explored = __ldcg(&ctl->explored);
+  const int status = __ldcg(&ctl->status);
   unsigned long long nf = 0, mf = 0, vd = 0;
 #pragma unroll
   for (int i = 0; i < kCounterShards; ++i) {
-    nf += *(volatile const unsigned long long *)&Rn->nf[i];
-    mf += *(volatile const unsigned long long *)&Rn->mf[i];
-    vd += *(volatile const unsigned long long *)&Rn->visdeg[i];
+    nf += nfs[i];
+    mf += mfs[i];
+    vd += vds[i];
   }
   cg_stats *st = p.stats;
   const long long now = global_ns();
   if (L < CG_HISTORY) {
     st->nf_history[L] = (int64_t)nf;
     st->direction_history[L] = dir;
-    st->round_ns[L] = now - ctl->t_round;
+    st->round_ns[L] = now - t_round;
   }
   ctl->t_round = now;
-  if (dir == kPull) ctl->pull_rounds += 1;
-  ctl->visited += nf;
+  const int pulls = pull_rounds + (dir == kPull ? 1 : 0);
+  ctl->pull_rounds = pulls;
+  const unsigned long long vis_total = visited + nf;
+  ctl->visited = vis_total;
   bool done = nf == 0;
+  int stat = status;
   if (!done && L + 1 >= p.level_cap) {
     atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
+    if (stat == 0) stat = CG_ERR_LEVEL_CAP;
     done = true;
   }
-  const int next = next_direction(p, dir, nf, ctl->prev_nf, mf, ctl->explored);
-  ctl->explored += vd;
+  const int next = next_direction(p, dir, nf, prev_nf, mf, explored);
+  ctl->explored = explored + vd;
   ctl->prev_nf = nf;
-  if (!done && next != dir) ctl->switches += 1;
+  const int sw = switches + ((!done && next != dir) ? 1 : 0);
+  ctl->switches = sw;
   RoundRec *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
   for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->mf[i] = Rz->visdeg[i] = 0;
   Rz->big = 0;
   Rz->nlight = Rz->work = 0;
   if (done) {
     const int rounds = L + 1;
-    st->status = *(volatile int *)&ctl->status;
+    st->status = stat;
     st->rounds = rounds;
-    st->visited = (int64_t)ctl->visited;
-    st->pull_rounds = ctl->pull_rounds;
-    st->switches = ctl->switches;
+    st->visited = (int64_t)vis_total;
+    st->pull_rounds = pulls;
+    st->switches = sw;
     st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
     st->finish_ns = 0;
     st->device_ms = 0.f;
