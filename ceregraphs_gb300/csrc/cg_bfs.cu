@@ -381,8 +381,13 @@ __device__ __forceinline__ int next_direction(const BfsParams &p, int dir, unsig
       return (dir == kPull || (long long)nf > p.tau) ? kPull : kPush;
     default: {
       if (dir == kPush) {
+        // Beamer's rule, plus a floor: a pull round walks every vertex's
+        // visited word, so a frontier whose edges are fewer than n / 8 stays
+        // push (near the end "unexplored" counts only unreachable edges)
         const double unexplored = (double)p.nnz - (double)explored;
-        return ((double)mf > unexplored / (double)p.alpha) ? kPull : kPush;
+        return ((double)mf > unexplored / (double)p.alpha && (double)mf > (double)p.n / 8.0)
+                   ? kPull
+                   : kPush;
       }
       const bool shrinking = nf < prev_nf;
       return (shrinking && (double)nf < (double)p.n / (double)p.beta) ? kPush : kPull;
