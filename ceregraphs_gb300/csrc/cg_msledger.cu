@@ -223,7 +223,7 @@ __device__ __forceinline__ uint32_t *claims(const MsParams &p, int L) {
 // hub in-lists by chunks (ORed into hub_found, merged after the wait).
 template <int W>
 __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
-                        const Mask<W> &active, MsRound *Rn, MsAcc &acc) {
+                        const Mask<W> &active, MsRound *Rc, MsRound *Rn, MsAcc &acc) {
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
   int32_t *q = next_parity ? p.queue1 : p.queue0;
@@ -260,51 +260,67 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     if (lane == 0 && cm) atomicOr(tnext + (base >> 5), cm);
     ms_enqueue<false>(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
   }
-  const int nwarps = (int)(nthreads >> 5);
-  for (int64_t j = warp_id_global(); j < p.nmed; j += nwarps) {
-    const int32_t v = p.med_vtx[j];
-    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
-    if (!want.any()) continue;
-    // medium vertex j has candidate slot j: its parents of this round go there
-    const Mask<W> got = or_warp_first<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1), want,
-                                         cur, p.cand + j * (64 * W), false);
-    const bool claimed = lane == 0 && got.any();
-    int64_t deg = 0;
-    if (claimed) {
-      st_mask<W>(nxt, v, got);
-      atomicOr(tnext + (v >> 5), 1u << (v & 31));
-      acc_lanes<W>(acc, got);
-      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
-    }
-    ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
-  }
-  if (p.nhub == 0) return;
-  const unsigned nchunks = p.hub_choff[p.nhub];
-  for (unsigned c = (unsigned)warp_id_global(); c < nchunks; c += (unsigned)nwarps) {
-    unsigned lo = 0, hi = (unsigned)p.nhub - 1;
-    while (lo < hi) {
-      const unsigned mid = (lo + hi + 1) >> 1;
-      if (p.hub_choff[mid] <= c)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const int h = (int)lo;
-    const int32_t v = p.hub_vtx[h];
-    const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
-    if (!want.any()) continue;
-    const int64_t s = __ldg(p.in_off + v) + (int64_t)(c - p.hub_choff[h]) * kHubChunk;
-    const int64_t e = min(s + (int64_t)kHubChunk, __ldg(p.in_off + v + 1));
-    // hub h has candidate slot nmed + h; several warps scan its chunks
-    const Mask<W> got = or_warp_first<W>(p, s, e, want, cur,
-                                         p.cand + (p.nmed + h) * (64 * W), true);
-    if (lane == 0) {
+  // medium vertices (groups of kMedGrab) then hub chunks (groups of
+  // kHubGrab), handed out dynamically -- one item per warp, then a counter --
+  // so that the round's last warps are not the ones with the longest lists
+  constexpr unsigned kMedGrab = 8, kHubGrab = 4;
+  const unsigned nwarps = (unsigned)(nthreads >> 5);
+  const unsigned nmg = (unsigned)((p.nmed + kMedGrab - 1) / kMedGrab);
+  const unsigned nchunks = p.nhub > 0 ? p.hub_choff[p.nhub] : 0u;
+  const unsigned nhg = (nchunks + kHubGrab - 1) / kHubGrab;
+  unsigned item = (unsigned)warp_id_global();
+  while (item < nmg + nhg) {
+    if (item < nmg) {
+      const int64_t j1 = min((int64_t)(item + 1) * kMedGrab, p.nmed);
+      for (int64_t j = (int64_t)item * kMedGrab; j < j1; ++j) {
+        const int32_t v = p.med_vtx[j];
+        const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
+        if (!want.any()) continue;
+        // medium vertex j has candidate slot j: its parents of this round go there
+        const Mask<W> got = or_warp_first<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1),
+                                             want, cur, p.cand + j * (64 * W), false);
+        const bool claimed = lane == 0 && got.any();
+        int64_t deg = 0;
+        if (claimed) {
+          st_mask<W>(nxt, v, got);
+          atomicOr(tnext + (v >> 5), 1u << (v & 31));
+          acc_lanes<W>(acc, got);
+          deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+        }
+        ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+      }
+    } else {
+      const unsigned c1 = min((item - nmg + 1) * kHubGrab, nchunks);
+      for (unsigned c = (item - nmg) * kHubGrab; c < c1; ++c) {
+        unsigned lo = 0, hi = (unsigned)p.nhub - 1;
+        while (lo < hi) {
+          const unsigned mid = (lo + hi + 1) >> 1;
+          if (p.hub_choff[mid] <= c)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        const int h = (int)lo;
+        const int32_t v = p.hub_vtx[h];
+        const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
+        if (!want.any()) continue;
+        const int64_t s = __ldg(p.in_off + v) + (int64_t)(c - p.hub_choff[h]) * kHubChunk;
+        const int64_t e = min(s + (int64_t)kHubChunk, __ldg(p.in_off + v + 1));
+        // hub h has candidate slot nmed + h; several warps scan its chunks
+        const Mask<W> got = or_warp_first<W>(p, s, e, want, cur,
+                                             p.cand + (p.nmed + h) * (64 * W), true);
+        if (lane == 0) {
 #pragma unroll
-      for (int j = 0; j < W; ++j)
-        if (got.w[j])
-          atomicOr(reinterpret_cast<unsigned long long *>(p.hub_found + (int64_t)h * W + j),
-                   (unsigned long long)got.w[j]);
+          for (int w = 0; w < W; ++w)
+            if (got.w[w])
+              atomicOr(reinterpret_cast<unsigned long long *>(p.hub_found + (int64_t)h * W + w),
+                       (unsigned long long)got.w[w]);
+        }
+      }
     }
+    unsigned nextitem = 0;
+    if (lane == 0) nextitem = nwarps + atomicAdd(&Rc->work, 1u);
+    item = __shfl_sync(kMsFull, nextitem, 0);
   }
 }
 
@@ -712,7 +728,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
       Mask<W> active;
 #pragma unroll
       for (int i = 0; i < W; ++i) active.w[i] = *(volatile unsigned long long *)&Rc->lanes[i];
-      lg_pull<W>(p, L, cur, nxt, active, Rn, acc);
+      lg_pull<W>(p, L, cur, nxt, active, Rc, Rn, acc);
       if (p.nhub > 0) {
         if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
         lg_hub_merge<W>(p, L, nxt, Rn, acc);
