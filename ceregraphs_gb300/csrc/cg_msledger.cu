@@ -230,49 +230,56 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
   uint32_t *tnext = claims(p, L + 1);
   const int lane = lane_id();
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
-       base < p.n; base += nthreads) {
-    const int64_t v = base + lane;
-    Mask<W> want = Mask<W>::zero();
-    int64_t s = 0, e = 0;
-    if (v < p.n) {
-      const Mask<W> fv = ld_mask<W>(cur, v);
-      const Mask<W> seen = ld_mask<W>(p.vis, v) | fv;
-      if (fv.any()) st_mask<W>(p.vis, v, seen);
-      want = active.andnot(seen);
-      if (want.any()) {
-        s = __ldg(p.in_off + v);
-        e = __ldg(p.in_off + v + 1);
-        if (e - s > kPullLight) want = Mask<W>::zero();  // medium list or hub chunks
-      }
-    }
-    if (!__ballot_sync(kMsFull, want.any())) continue;
-    Mask<W> got = Mask<W>::zero();
-    if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur);
-    const bool claimed = got.any();
-    int64_t deg = 0;
-    if (claimed) {
-      st_mask<W>(nxt, v, got);
-      acc_lanes<W>(acc, got);
-      deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
-    }
-    const unsigned cm = __ballot_sync(kMsFull, claimed);
-    if (lane == 0 && cm) atomicOr(tnext + (base >> 5), cm);
-    ms_enqueue<false>(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
-  }
-  // medium vertices (groups of kMedGrab) then hub chunks (groups of
-  // kHubGrab), handed out dynamically -- one item per warp, then a counter --
-  // so that the round's last warps are not the ones with the longest lists
-  constexpr unsigned kMedGrab = 8, kHubGrab = 4;
+  // light vertex groups (kLightGrab x 32 vertices), then medium vertices
+  // (groups of kMedGrab), then hub chunks (groups of kHubGrab), handed out
+  // dynamically -- one item per warp, then a counter -- so that the round's
+  // last warps are not the ones with the longest lists
+  constexpr unsigned kLightGrab = 8, kMedGrab = 8, kHubGrab = 4;
   const unsigned nwarps = (unsigned)(nthreads >> 5);
+  const unsigned nlg = (unsigned)((p.n + 32 * kLightGrab - 1) / (32 * kLightGrab));
   const unsigned nmg = (unsigned)((p.nmed + kMedGrab - 1) / kMedGrab);
   const unsigned nchunks = p.nhub > 0 ? p.hub_choff[p.nhub] : 0u;
   const unsigned nhg = (nchunks + kHubGrab - 1) / kHubGrab;
   unsigned item = (unsigned)warp_id_global();
-  while (item < nmg + nhg) {
-    if (item < nmg) {
-      const int64_t j1 = min((int64_t)(item + 1) * kMedGrab, p.nmed);
-      for (int64_t j = (int64_t)item * kMedGrab; j < j1; ++j) {
+  while (item < nlg + nmg + nhg) {
+    // the next item is claimed before this one is worked, hiding the atomic
+    unsigned nextitem = 0;
+    if (lane == 0) nextitem = nwarps + atomicAdd(&Rc->work, 1u);
+    if (item < nlg) {
+      const int64_t b1 = min((int64_t)(item + 1) * 32 * kLightGrab, p.n);
+      for (int64_t base = (int64_t)item * 32 * kLightGrab; base < b1; base += 32) {
+        const int64_t v = base + lane;
+        Mask<W> want = Mask<W>::zero();
+        int64_t s = 0, e = 0;
+        if (v < p.n) {
+          const Mask<W> fv = ld_mask<W>(cur, v);
+          const Mask<W> seen = ld_mask<W>(p.vis, v) | fv;
+          if (fv.any()) st_mask<W>(p.vis, v, seen);
+          want = active.andnot(seen);
+          if (want.any()) {
+            s = __ldg(p.in_off + v);
+            e = __ldg(p.in_off + v + 1);
+            if (e - s > kPullLight) want = Mask<W>::zero();  // medium list or hub chunks
+          }
+        }
+        if (!__ballot_sync(kMsFull, want.any())) continue;
+        Mask<W> got = Mask<W>::zero();
+        if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur);
+        const bool claimed = got.any();
+        int64_t deg = 0;
+        if (claimed) {
+          st_mask<W>(nxt, v, got);
+          acc_lanes<W>(acc, got);
+          deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+        }
+        const unsigned cm = __ballot_sync(kMsFull, claimed);
+        if (lane == 0 && cm) atomicOr(tnext + (base >> 5), cm);
+        ms_enqueue<false>(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+      }
+    } else if (item < nlg + nmg) {
+      const unsigned mi = item - nlg;
+      const int64_t j1 = min((int64_t)(mi + 1) * kMedGrab, p.nmed);
+      for (int64_t j = (int64_t)mi * kMedGrab; j < j1; ++j) {
         const int32_t v = p.med_vtx[j];
         const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
         if (!want.any()) continue;
@@ -290,8 +297,9 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
       }
     } else {
-      const unsigned c1 = min((item - nmg + 1) * kHubGrab, nchunks);
-      for (unsigned c = (item - nmg) * kHubGrab; c < c1; ++c) {
+      const unsigned hi_item = item - nlg - nmg;
+      const unsigned c1 = min((hi_item + 1) * kHubGrab, nchunks);
+      for (unsigned c = hi_item * kHubGrab; c < c1; ++c) {
         unsigned lo = 0, hi = (unsigned)p.nhub - 1;
         while (lo < hi) {
           const unsigned mid = (lo + hi + 1) >> 1;
@@ -318,8 +326,6 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         }
       }
     }
-    unsigned nextitem = 0;
-    if (lane == 0) nextitem = nwarps + atomicAdd(&Rc->work, 1u);
     item = __shfl_sync(kMsFull, nextitem, 0);
   }
 }
