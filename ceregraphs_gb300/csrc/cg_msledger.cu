@@ -47,9 +47,13 @@ namespace {
 constexpr int kOutBlock = 128;                 // output pass: 4 warps a block
 constexpr int kOutWarps = kOutBlock / 32;
 constexpr int kOutLevels = 4;                  // levels resolved per in-list scan
-constexpr int kParStride = 65;                 // shared row strides (bank-conflict free)
-constexpr int kLvlStride = 68;
-constexpr int kOutWarpBytes = 32 * kParStride * 4 + 32 * kLvlStride;
+constexpr int kParStride = 65;                 // shared row stride (bank-conflict free)
+constexpr int kOutWarpBytes = 32 * kParStride * 4;
+constexpr int kSlices = 7;                     // bit slices of a level (levels 0..64)
+
+// Bits 0..3 of x moved to bit 0 of bytes 0..3 (the four shifted copies do not
+// overlap, so the product has no carries).
+__device__ __forceinline__ uint32_t spread4(uint32_t x) { return (x * 0x00204081u) & 0x01010101u; }
 
 template <int W>
 __device__ __forceinline__ uint64_t *plane(const MsParams &p, int L) {
@@ -816,12 +820,13 @@ __device__ __forceinline__ uint64_t parent_hits(const MsParams &p, int32_t u, in
 
 // Output pass.  Each warp takes 32 consecutive vertices (one per thread).  Per
 // 64-lane half of the batch a thread reads its vertex's history masks once
-// and records each lane's level as a byte of a shared tile row (0xFF =
-// unreached); parents of levels >= 2 go to a second tile: the slot's
-// candidates (in-degree > kPullLight, copied by the warp) or the first hit of
-// the thread's scan of its own short in-list.  Then, lane by lane, the warp
-// writes the tile's 32 levels and 32 parents as two 128-byte rows; parents of
-// levels 0 and 1 are the vertex and the lane's root.
+// and keeps each lane's level as bit slices in registers; parents of levels
+// >= 2 go to a shared tile row: the slot's candidates (in-degree >
+// kPullLight, copied by the warp), the pull rounds' first-hit records, or the
+// hits of the thread's scan of its own short in-list (the largest of these
+// masks stays a register mask).  Then, lane by lane, the warp writes the
+// tile's 32 levels and 32 parents as two 128-byte rows; parents of levels 0
+// and 1 are the vertex and the lane's root.
 template <int W>
 __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   extern __shared__ __align__(16) unsigned char s_tile[];
@@ -846,9 +851,7 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
   int32_t *par = reinterpret_cast<int32_t *>(s_tile + wib * kOutWarpBytes);
-  uint8_t *lvl = s_tile + wib * kOutWarpBytes + 32 * kParStride * 4;
   int32_t *my_par = par + lane * kParStride;
-  uint8_t *my_lvl = lvl + lane * kLvlStride;
   const int64_t nwarps = (int64_t)gridDim.x * kOutWarps;
   for (int64_t tile = (int64_t)blockIdx.x * kOutWarps + wib; tile * 32 < p.n; tile += nwarps) {
     const int64_t v = tile * 32 + lane;
@@ -891,11 +894,12 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
           }
         }
       }
-      // level bytes; the first kOutLevels levels >= 2 of a light vertex for its
+      // each lane's level as bit slices (bit l of S[b] = bit b of lane l's
+      // level); the first kOutLevels levels >= 2 of a light vertex for its
       // scan, any further ones (rare) through collect_levels below
-      uint32_t *lw = reinterpret_cast<uint32_t *>(my_lvl);
+      uint64_t S[kSlices], reached = 0;
 #pragma unroll
-      for (int i = 0; i < 16; ++i) lw[i] = 0xffffffffu;
+      for (int b = 0; b < kSlices; ++b) S[b] = 0;
       int Ls[kOutLevels];
       uint64_t Ms[kOutLevels];
       int nl = 0;
@@ -927,37 +931,35 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
           }
         }
       }
-      if (valid) {
-        for (int L0 = 0; L0 < rounds; L0 += kPre) {
-          uint64_t pm[kPre];
+      for (int L0 = 0; L0 < rounds; L0 += kPre) {  // uniform: the whole warp
+        uint64_t pm[kPre];
 #pragma unroll
-          for (int j = 0; j < kPre; ++j)
-            pm[j] = L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] : 0ull;
+        for (int j = 0; j < kPre; ++j)
+          pm[j] = valid && L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] : 0ull;
 #pragma unroll
-          for (int j = 0; j < kPre; ++j) {
-            uint64_t m = pm[j];
-            const int L = L0 + j;
-            if (m) atomicAdd(&s_cnt[L], (unsigned long long)__popcll(m));
-            const uint64_t scan = m & ~covered;
-            if (scan && L >= 2 && slot < 0) {
-              if (nl < kOutLevels) {
+        for (int j = 0; j < kPre; ++j) {
+          const uint64_t m = pm[j];
+          const int L = L0 + j;
+          const unsigned c = __reduce_add_sync(kMsFull, (unsigned)__popcll(m));
+          if (lane == 0 && c) atomicAdd(&s_cnt[L], (unsigned long long)c);
+          reached |= m;
 #pragma unroll
-                for (int k = 0; k < kOutLevels; ++k)
-                  if (k == nl) {
-                    Ls[k] = L;
-                    Ms[k] = scan;
-                  }
-                ++nl;
-                gtodo |= scan;
-                last = L;
-              } else {
-                rest |= scan;
-              }
-            }
-            while (m) {
-              const int b = __ffsll((long long)m) - 1;
-              m &= m - 1;
-              my_lvl[b] = (uint8_t)L;
+          for (int b = 0; b < kSlices; ++b)
+            if ((L >> b) & 1) S[b] |= m;
+          const uint64_t scan = m & ~covered;
+          if (scan && L >= 2 && slot < 0) {
+            if (nl < kOutLevels) {
+#pragma unroll
+              for (int k = 0; k < kOutLevels; ++k)
+                if (k == nl) {
+                  Ls[k] = L;
+                  Ms[k] = scan;
+                }
+              ++nl;
+              gtodo |= scan;
+              last = L;
+            } else {
+              rest |= scan;
             }
           }
         }
@@ -1003,23 +1005,63 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
           if (!gtodo) rest = 0;
         }
       }
-      __syncwarp();
-      // rows: lane l of this half, vertices tile*32 .. tile*32 + 31
-      const int lanes = min(64, p.k - 64 * h);
-#pragma unroll 4
-      for (int l = 0; l < lanes; ++l) {
-        const uint8_t lv = my_lvl[l];
-        int32_t pv = my_par[l];
-        if ((m_first >> l) & 1ull) pv = u_first;
+      // the largest first-hit mask (scan or pull record) is applied lane by
+      // lane below; the others go into the tile row now
+      int32_t d = u_first;
+      uint64_t dm = m_first;
+      {
+        int best = -1, bc = __popcll(m_first);
+#pragma unroll
+        for (int q = 0; q < kPairs; ++q) {
+          const int c = __popcll(pmk[q]);
+          if (c > bc) {
+            bc = c;
+            best = q;
+          }
+        }
+        if (best >= 0) {
+          for (uint64_t x = m_first; x; x &= x - 1) my_par[__ffsll((long long)x) - 1] = u_first;
+#pragma unroll
+          for (int q = 0; q < kPairs; ++q)
+            if (q == best) {
+              d = pu[q];
+              dm = pmk[q];
+            }
+        }
 #pragma unroll
         for (int q = 0; q < kPairs; ++q)
-          if ((pmk[q] >> l) & 1ull) pv = pu[q];
-        if (lv == 1) pv = p.roots[64 * h + l];
-        if (lv == 0) pv = (int32_t)v;
-        const int64_t at = (int64_t)(64 * h + l) * p.n + v;
-        if (valid) {
-          p.levels[at] = lv == 0xff ? -1 : (int32_t)lv;
-          p.parents[at] = lv == 0xff ? -1 : pv;
+          if (q != best)
+            for (uint64_t x = pmk[q]; x; x &= x - 1) my_par[__ffsll((long long)x) - 1] = pu[q];
+      }
+      __syncwarp();
+      // rows: lane l of this half, vertices tile*32 .. tile*32 + 31; four
+      // lanes' levels built at a time as the bytes of a word (0xFF unreached)
+      const int lanes = min(64, p.k - 64 * h);
+      int nsl = 1;
+      while (nsl < kSlices && (rounds - 1) >> nsl) ++nsl;
+      int32_t *out_l = p.levels + (int64_t)(64 * h) * p.n + v;
+      int32_t *out_p = p.parents + (int64_t)(64 * h) * p.n + v;
+      for (int l4 = 0; l4 < lanes; l4 += 4) {
+        uint32_t word = spread4(~(uint32_t)(reached >> l4) & 0xFu) * 0xFFu;
+#pragma unroll
+        for (int b = 0; b < kSlices; ++b)
+          if (b < nsl) word |= spread4((uint32_t)(S[b] >> l4) & 0xFu) << b;
+        const uint32_t dq = (uint32_t)(dm >> l4);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int l = l4 + i;
+          if (l < lanes) {
+            const uint32_t lv = (word >> (8 * i)) & 0xFFu;
+            int32_t pv = (dq >> i) & 1u ? d : my_par[l];
+            if (lv == 1) pv = p.roots[64 * h + l];
+            if (lv == 0) pv = (int32_t)v;
+            if (valid) {
+              *out_l = lv == 0xFFu ? -1 : (int32_t)lv;
+              *out_p = lv == 0xFFu ? -1 : pv;
+            }
+            out_l += p.n;
+            out_p += p.n;
+          }
         }
       }
       __syncwarp();
