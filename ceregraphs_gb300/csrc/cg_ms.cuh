@@ -15,7 +15,8 @@ constexpr int kMsMaxLanes = 128;
 constexpr int kPullLight = 32;    // in-degree <= this: one thread scans the in-list
 constexpr int kHubDeg = 1024;     // in-degree > this: hub
 constexpr int kHubChunk = 1024;   // in-list entries of a hub per work item
-constexpr int kPairs = 4;         // first-hit records per light vertex (ledger batches)
+constexpr int kPairs = 4;         // first-hit records a light vertex's pull rounds may take
+constexpr int kRecords = 8;       // records per light vertex in all (pull rounds + scan pass)
 
 struct MsRound {
   unsigned long long nf[kCounterShards];      // vertices with a nonzero frontier mask
@@ -47,6 +48,7 @@ struct MsCtl {
   int pull_rounds;
   int switches;
   unsigned exited;                // blocks past the final pass (finish time)
+  unsigned nover;                 // light vertices whose records ran out (scan pass)
   unsigned long long visited;
   unsigned long long done[2];     // lanes whose search ended (cleared by the host)
   long long t_start;
@@ -63,6 +65,7 @@ struct MsParams {
   const int32_t *__restrict__ out_idx;
   uint64_t *vis, *fr0, *fr1, *fr2;
   uint32_t *touched0, *touched1, *touched2;
+  uint32_t *scanmap;  // light vertices with lanes their records leave open (ledger)
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
@@ -96,8 +99,9 @@ struct MsParams {
   const uint32_t *cand_choff; // [ncand + 1] prefix of in-list chunks
   uint32_t *cand;             // [ncand][64 W], 0xFFFFFFFF = none yet
   int ncand;
-  // first hits of light vertices' pull-round scans: up to kPairs (source,
-  // lanes) records per vertex, record q at [q * n + v]
+  // (source, lanes) records of light vertices: the first hits of their
+  // pull-round scans (up to kPairs), then those of the scan pass after the
+  // rounds (up to kRecords in all); record q at [q * n + v]
   int32_t *pair_u;
   uint64_t *pair_m;           // W words per record
   uint8_t *pair_n;            // [n] records used
@@ -592,6 +596,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.pair_m = s->pair_m;
   p.pair_n = s->pair_n;
   p.touched0 = s->touched;
+  p.scanmap = s->touched + 3 * p.words;
   p.touched1 = s->touched + p.words;
   p.touched2 = s->touched + 2 * p.words;
   p.queue0 = s->queue;

@@ -745,12 +745,12 @@ static int ms_build_cands(cg_graph *g, MsState *s) {
       cudaMalloc(&s->cand_vtx, sizeof(int32_t) * nc) != cudaSuccess ||
       cudaMalloc(&s->cand_choff, sizeof(uint32_t) * (nc + 1)) != cudaSuccess ||
       cudaMalloc(&s->cand, sizeof(uint32_t) * nc * 64 * s->lane_words) != cudaSuccess ||
-      cudaMalloc(&s->pair_u, sizeof(int32_t) * kPairs * (size_t)g->n) != cudaSuccess ||
-      cudaMalloc(&s->pair_m, sizeof(uint64_t) * kPairs * (size_t)g->n * s->lane_words) !=
+      cudaMalloc(&s->pair_u, sizeof(int32_t) * kRecords * (size_t)g->n) != cudaSuccess ||
+      cudaMalloc(&s->pair_m, sizeof(uint64_t) * kRecords * (size_t)g->n * s->lane_words) !=
           cudaSuccess ||
       cudaMalloc(&s->pair_n, (size_t)((g->n + 3) / 4) * 4) != cudaSuccess)
     return CG_ERR_OUT_OF_MEMORY;
-  g->device_bytes += (sizeof(int32_t) + sizeof(uint64_t) * s->lane_words) * kPairs * g->n + g->n;
+  g->device_bytes += (sizeof(int32_t) + sizeof(uint64_t) * s->lane_words) * kRecords * g->n + g->n;
   CG_CUDA(cudaMemsetAsync(s->cand_slot, 0xff, sizeof(int32_t) * (size_t)g->n, g->stream));
   if (s->nmed)
     CG_CUDA(cudaMemcpyAsync(s->cand_vtx, s->med_vtx, sizeof(int32_t) * (size_t)s->nmed,
@@ -797,7 +797,7 @@ static int ms_create_state(cg_graph *g, int lane_words, int hist_planes, MsState
   const size_t bits = sizeof(uint64_t) * (1 + (size_t)s->hist_planes) * (size_t)g->n * lane_words;
   const size_t words = (size_t)((g->n + 31) / 32);
   if (cudaMalloc(&s->bits, bits) != cudaSuccess ||
-      cudaMalloc(&s->touched, sizeof(uint32_t) * 3 * words) != cudaSuccess ||
+      cudaMalloc(&s->touched, sizeof(uint32_t) * 4 * words) != cudaSuccess ||
       cudaMalloc(&s->queue, sizeof(int32_t) * 2 * (size_t)g->n) != cudaSuccess ||
       cudaMalloc(&s->bigoff, sizeof(uint32_t) * 2 * (size_t)s->bcap) != cudaSuccess ||
       cudaMalloc(&s->ctl, sizeof(MsCtl)) != cudaSuccess ||
@@ -811,7 +811,7 @@ static int ms_create_state(cg_graph *g, int lane_words, int hist_planes, MsState
     ms_free_state(s);
     return rc;
   }
-  g->device_bytes += bits + sizeof(uint32_t) * 3 * words + sizeof(int32_t) * 2 * g->n +
+  g->device_bytes += bits + sizeof(uint32_t) * 4 * words + sizeof(int32_t) * 2 * g->n +
                      sizeof(uint32_t) * 2 * s->bcap + sizeof(MsCtl);
   *out = s;
   return CG_OK;

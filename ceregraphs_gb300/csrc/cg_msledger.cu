@@ -47,13 +47,21 @@ namespace {
 constexpr int kOutBlock = 128;                 // output pass: 4 warps a block
 constexpr int kOutWarps = kOutBlock / 32;
 constexpr int kOutLevels = 4;                  // levels resolved per in-list scan
-constexpr int kParStride = 65;                 // shared row stride (bank-conflict free)
-constexpr int kOutWarpBytes = 32 * kParStride * 4;
+// A warp's shared tile: 32 rows of 64 parents, lane l of row t at column
+// l ^ t (each of the warp's threads reads its own row at the same lane: no
+// bank conflicts); then 32 rows of kRecords record sources, stride kPuStride.
+constexpr int kPuStride = 9;
+constexpr int kOutWarpBytes = 32 * 64 * 4 + 32 * kPuStride * 4;
 constexpr int kSlices = 7;                     // bit slices of a level (levels 0..64)
 
 // Bits 0..3 of x moved to bit 0 of bytes 0..3 (the four shifted copies do not
 // overlap, so the product has no carries).
 __device__ __forceinline__ uint32_t spread4(uint32_t x) { return (x * 0x00204081u) & 0x01010101u; }
+
+template <bool B>
+struct Flag {
+  static constexpr bool value = B;
+};
 
 template <int W>
 __device__ __forceinline__ uint64_t *plane(const MsParams &p, int L) {
@@ -82,11 +90,11 @@ __device__ __forceinline__ Mask<W> or_thread(const MsParams &p, int64_t s, int64
 // or_thread that also records, for light vertex v, each in-list entry that
 // brings new lanes -- their lowest-index parent, the scan being ascending --
 // as a (source, lanes) pair, up to kPairs per vertex over all pull rounds.
-// Lanes found after the records run out are left to the output pass's scan.
+// Lanes found after the records run out (`over`) are left to the scan pass.
 template <int W>
 __device__ __forceinline__ Mask<W> or_thread_rec(const MsParams &p, int64_t v, int64_t s,
                                                  int64_t e, const Mask<W> &want,
-                                                 const uint64_t *cur) {
+                                                 const uint64_t *cur, bool &over) {
   constexpr int G = 4;
   Mask<W> got = Mask<W>::zero();
   int used = p.pair_n[v];
@@ -107,6 +115,8 @@ __device__ __forceinline__ Mask<W> or_thread_rec(const MsParams &p, int64_t v, i
           p.pair_u[at] = u[k];
           st_mask<W>(p.pair_m, at, nb);
           ++used;
+        } else {
+          over = true;
         }
         got = got | nb;
       }
@@ -268,7 +278,10 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         }
         if (!__ballot_sync(kMsFull, want.any())) continue;
         Mask<W> got = Mask<W>::zero();
-        if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur);
+        bool over = false;
+        if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur, over);
+        const unsigned om = __ballot_sync(kMsFull, over);
+        if (lane == 0 && om) atomicOr(p.scanmap + (base >> 5), om);
         const bool claimed = got.any();
         int64_t deg = 0;
         if (claimed) {
@@ -684,6 +697,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     p.touched0[w] = 0;
     p.touched1[w] = 0;
     p.touched2[w] = 0;
+    p.scanmap[w] = 0;
   }
   uint32_t *pn = reinterpret_cast<uint32_t *>(p.pair_n);
   for (int64_t w = gtid; w < (p.n + 3) / 4; w += nthreads) pn[w] = 0;
@@ -721,7 +735,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     __syncthreads();
     ok = s_payload != kWaitFailed;
   }
-  int L = 0, dir = 0, ran = 0;
+  int L = 0, dir = 0, pdir = 0, ran = 0;
   MsAcc acc, tot;
   while (ok) {
     const uint64_t *cur = plane<W>(p, L);
@@ -734,6 +748,16 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     }
     uint32_t *tclr = claims(p, L + 2);
     for (int64_t w = gtid; w < p.words; w += nthreads) tclr[w] = 0;
+    if (L >= 2 && pdir == 0) {
+      // a push round gave these vertices lanes at level L >= 2: the scan
+      // pass resolves their parents (atomic: a pull round of this same
+      // round L may mark vertices of the same words)
+      const uint32_t *tcur = claims(p, L);
+      for (int64_t w = gtid; w < p.words; w += nthreads) {
+        const uint32_t t = tcur[w];
+        if (t) atomicOr(p.scanmap + w, t);
+      }
+    }
     if (dir == 1) {
       Mask<W> active;
 #pragma unroll
@@ -763,6 +787,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
       break;
     }
     if (payload & kMsStop) break;
+    pdir = dir;
     dir = (payload & kMsNextPull) ? 1 : 0;
     ++L;
     ++ran;
@@ -771,38 +796,19 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     p.stats->status = *(volatile int *)&ctl->status;
 }
 
-// ---- output pass ----------------------------------------------------------
+// ---- scan pass, output pass, fix-up pass ------------------------------------
 
-// Up to kOutLevels levels >= `from` holding lanes of `todo` at vertex v (half
-// h of the lanes), ascending: Ls[k] the level, Ms[k] its lanes.  Advances
-// `from` past the last one taken; returns the lanes taken.
-template <int W>
-__device__ __forceinline__ uint64_t collect_levels(const MsParams &p, int64_t v, int h, int rounds,
-                                                   uint64_t todo, int &from, int (&Ls)[kOutLevels],
-                                                   uint64_t (&Ms)[kOutLevels]) {
-#pragma unroll
-  for (int k = 0; k < kOutLevels; ++k) {
-    Ls[k] = 1;
-    Ms[k] = 0;
-  }
-  uint64_t covered = 0;
-  int nl = 0;
-  for (int L = from; L < rounds && nl < kOutLevels && todo; ++L) {
-    const uint64_t m = plane<W>(p, L)[v * W + h] & todo;
-    if (m) {
-#pragma unroll
-      for (int k = 0; k < kOutLevels; ++k)
-        if (k == nl) {
-          Ls[k] = L;
-          Ms[k] = m;
-        }
-      covered |= m;
-      todo &= ~m;
-      ++nl;
-    }
-    from = L + 1;
-  }
-  return covered;
+constexpr int kScanBlock = 256;  // scan and fix-up passes: threads a block
+constexpr int kScanWords = 8;    // scan pass: scanmap words a warp takes at a time
+constexpr int kScanG = 4;        // in-list entries loaded together
+constexpr int kPre = 8;          // history planes loaded together (the output pass needs 8)
+
+// The planes the rounds filled: F_0 .. F_{rounds - 1} (F_rounds is empty).
+__device__ __forceinline__ int history_rounds(const MsParams &p) {
+  int rounds = *(volatile int *)&p.ctl->L;
+  if (rounds > p.hist_planes) rounds = p.hist_planes;
+  if (rounds > CG_HISTORY + 1) rounds = CG_HISTORY + 1;
+  return rounds;
 }
 
 // Lanes of `want` for which u is one level closer to the root than v: bit l
@@ -818,21 +824,177 @@ __device__ __forceinline__ uint64_t parent_hits(const MsParams &p, int32_t u, in
   return b & want;
 }
 
+// The lanes of `todo` (half h) that light vertex v reached at a level >= 2,
+// resolved by scans of v's ascending in-list: the first entry u holding the
+// lane in F_{level - 1}[u] is the lane's parent, the lowest-index rule.  One
+// pass over the list resolves up to kOutLevels levels; hit(u, lanes) gets
+// each entry that resolves lanes.
+template <int W, class Hit>
+__device__ __forceinline__ void scan_in_list(const MsParams &p, int64_t v, int h, int rounds,
+                                             int64_t s, int64_t e, uint64_t todo, Hit &&hit) {
+  int L = 2;
+  while (todo && L < rounds) {
+    int Ls[kOutLevels];
+    uint64_t Ms[kOutLevels];
+#pragma unroll
+    for (int k = 0; k < kOutLevels; ++k) {
+      Ls[k] = 1;
+      Ms[k] = 0;
+    }
+    int nl = 0;
+    uint64_t gtodo = 0;
+    while (nl < kOutLevels && L < rounds && todo) {
+      uint64_t pm[kPre];
+#pragma unroll
+      for (int j = 0; j < kPre; ++j)
+        pm[j] = L + j < rounds ? plane<W>(p, L + j)[v * W + h] : 0ull;
+      int taken = 0;
+#pragma unroll
+      for (int j = 0; j < kPre; ++j) {
+        if (nl < kOutLevels) {
+          const uint64_t m = pm[j] & todo;
+          if (m) {
+#pragma unroll
+            for (int k = 0; k < kOutLevels; ++k)
+              if (k == nl) {
+                Ls[k] = L + j;
+                Ms[k] = m;
+              }
+            ++nl;
+            todo &= ~m;
+            gtodo |= m;
+          }
+          taken = j + 1;
+        }
+      }
+      L += taken;
+    }
+    for (int64_t j0 = s; j0 < e && gtodo; j0 += kScanG) {
+      int32_t u[kScanG];
+      uint64_t b[kScanG];
+#pragma unroll
+      for (int k = 0; k < kScanG; ++k) u[k] = j0 + k < e ? __ldg(p.in_idx + j0 + k) : -1;
+#pragma unroll
+      for (int k = 0; k < kScanG; ++k)
+        b[k] = u[k] >= 0 ? parent_hits<W>(p, u[k], h, Ls, Ms, gtodo) : 0;
+#pragma unroll
+      for (int k = 0; k < kScanG; ++k) {
+        const uint64_t bk = b[k] & gtodo;
+        if (bk) {
+          gtodo &= ~bk;
+          hit(u[k], bk);
+        }
+      }
+    }
+  }
+}
+
+// OR of the masks of records [0, np) of vertex v, half h.
+template <int W>
+__device__ __forceinline__ uint64_t records_mask(const MsParams &p, int64_t v, int h, int np) {
+  uint64_t m = 0;
+#pragma unroll
+  for (int q = 0; q < kRecords; ++q)
+    if (q < np) m |= p.pair_m[((int64_t)q * p.n + v) * W + h];
+  return m;
+}
+
+// Scan pass, between the rounds and the output pass, over the light vertices
+// (in-degree 1 .. kPullLight; heavier ones have candidate slots) that the
+// rounds marked in scanmap: reached by a push round at a level >= 2, or with
+// more pull-round first hits than records.  A warp takes kScanWords words of
+// the map, compacts their marked vertices in shared memory, and gives each
+// thread one.
+// The lanes a vertex's records leave open are resolved by scan_in_list and
+// appended as records; a vertex that runs out of records goes on a list
+// (queue0, free once the rounds are over) for the fix-up pass.
+template <int W>
+__global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
+  __shared__ int32_t s_list[kScanBlock / 32][kScanWords * 32];
+  if (*(volatile int *)p.flag || *(volatile int *)&p.ctl->status != 0) return;
+  const int rounds = history_rounds(p);
+  if (rounds <= 2) return;
+  const int lane = lane_id();
+  int32_t *list = s_list[threadIdx.x >> 5];
+  const int64_t nwarps = (int64_t)gridDim.x * (kScanBlock / 32);
+  for (int64_t w0 = warp_id_global() * kScanWords; w0 < p.words; w0 += nwarps * kScanWords) {
+    const int64_t wi = w0 + lane;
+    uint32_t bits = lane < kScanWords && wi < p.words ? p.scanmap[wi] : 0u;
+    const int c = __popc(bits);
+    int incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(kMsFull, incl, d);
+      if (lane >= d) incl += y;
+    }
+    const int total = __shfl_sync(kMsFull, incl, 31);
+    for (int at = incl - c; bits; bits &= bits - 1) list[at++] = (int32_t)(wi * 32 + __ffs(bits) - 1);
+    __syncwarp();
+    for (int i = lane; i < total; i += 32) {
+      const int64_t v = list[i];
+      const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+      if (e == s || e - s > kPullLight) continue;
+      const int np0 = p.pair_n[v];
+      int np = np0;
+      bool over = false;
+      for (int h = 0; h < W && 64 * h < p.k; ++h) {
+        const uint64_t covered = records_mask<W>(p, v, h, np0);
+        scan_in_list<W>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
+          if (np < kRecords) {
+            const int64_t at = (int64_t)np * p.n + v;
+            p.pair_u[at] = u;
+#pragma unroll
+            for (int w = 0; w < W; ++w) p.pair_m[at * W + w] = w == h ? m : 0ull;
+            ++np;
+          } else {
+            over = true;
+          }
+        });
+      }
+      if (np != np0) p.pair_n[v] = (uint8_t)np;
+      if (over) p.queue0[atomicAdd(&p.ctl->nover, 1u)] = (int32_t)v;
+    }
+    __syncwarp();
+  }
+}
+
+// Fix-up pass, after the output pass: the lanes of the listed vertices that
+// no record covers get their parents written one by one (a vertex with more
+// distinct parents than kRecords; rare).
+template <int W>
+__global__ void __launch_bounds__(kScanBlock) msbfs_fixup(MsParams p) {
+  if (*(volatile int *)p.flag || *(volatile int *)&p.ctl->status != 0) return;
+  const unsigned cnt = *(volatile unsigned *)&p.ctl->nover;
+  if (cnt == 0) return;
+  const int rounds = history_rounds(p);
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += nthreads) {
+    const int64_t v = p.queue0[i];
+    const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+    const int np = p.pair_n[v];
+    for (int h = 0; h < W && 64 * h < p.k; ++h) {
+      const uint64_t covered = records_mask<W>(p, v, h, np);
+      scan_in_list<W>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
+        for (uint64_t x = m; x; x &= x - 1)
+          p.parents[(int64_t)(64 * h + __ffsll((long long)x) - 1) * p.n + v] = u;
+      });
+    }
+  }
+}
+
 // Output pass.  Each warp takes 32 consecutive vertices (one per thread).  Per
 // 64-lane half of the batch a thread reads its vertex's history masks once
 // and keeps each lane's level as bit slices in registers; parents of levels
-// >= 2 go to a shared tile row: the slot's candidates (in-degree >
-// kPullLight, copied by the warp), the pull rounds' first-hit records, or the
-// hits of the thread's scan of its own short in-list (the largest of these
-// masks stays a register mask).  Then, lane by lane, the warp writes the
-// tile's 32 levels and 32 parents as two 128-byte rows; parents of levels 0
-// and 1 are the vertex and the lane's root.
+// >= 2 come from the slot's candidates (in-degree > kPullLight), copied by
+// the warp into the vertex's shared tile row, or from the vertex's (source,
+// lanes) records: their sources in a shared table, each lane's record index
+// as bit slices like the levels.  Then, lane by lane,
+// the warp writes the tile's 32 levels and 32 parents as two 128-byte rows;
+// parents of levels 0 and 1 are the vertex and the lane's root.
 template <int W>
 __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   extern __shared__ __align__(16) unsigned char s_tile[];
-  __shared__ unsigned long long s_cnt[CG_HISTORY + 1];  // lane discoveries per level
-  constexpr int kPre = 8;     // history planes loaded together
-  constexpr int kScanG = 8;   // in-list entries loaded together
+  __shared__ unsigned s_cnt[CG_HISTORY + 1];  // lane discoveries per level
   MsCtl *ctl = p.ctl;
   if (*(volatile int *)p.flag) {
     // the gated direct launch that follows needs a clean control block
@@ -843,26 +1005,22 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
     return;
   }
   if (*(volatile int *)&ctl->status != 0) return;  // timed out or over the level cap
-  int rounds = *(volatile int *)&ctl->L;           // F_0 .. F_rounds, F_rounds empty
-  if (rounds > p.hist_planes) rounds = p.hist_planes;
-  if (rounds > CG_HISTORY + 1) rounds = CG_HISTORY + 1;
+  const int rounds = history_rounds(p);
   for (int i = threadIdx.x; i <= CG_HISTORY; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
   int32_t *par = reinterpret_cast<int32_t *>(s_tile + wib * kOutWarpBytes);
-  int32_t *my_par = par + lane * kParStride;
+  int32_t *my_row = par + lane * 64;  // lane l at my_row[l ^ lane]
+  int32_t *my_pu = par + 32 * 64 + lane * kPuStride;
+  int nsl = 1;  // bit slices needed for levels 0 .. rounds - 1
+  while (nsl < kSlices && (rounds - 1) >> nsl) ++nsl;
   const int64_t nwarps = (int64_t)gridDim.x * kOutWarps;
   for (int64_t tile = (int64_t)blockIdx.x * kOutWarps + wib; tile * 32 < p.n; tile += nwarps) {
     const int64_t v = tile * 32 + lane;
     const bool valid = v < p.n;
-    int64_t s = 0, e = 0;
-    int slot = -1;
-    if (valid) {
-      s = __ldg(p.in_off + v);
-      e = __ldg(p.in_off + v + 1);
-      slot = p.cand_slot[v];
-    }
+    const int slot = valid ? p.cand_slot[v] : -1;
+    const int np = valid && slot < 0 ? p.pair_n[v] : 0;
 #pragma unroll 1
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
       // parents of levels >= 2 of the tile's slotted vertices: the warp copies
@@ -888,180 +1046,123 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
             if (src[r] >= 0) {
-              par[src[r] * kParStride + 2 * lane] = (int32_t)x[r].x;
-              par[src[r] * kParStride + 2 * lane + 1] = (int32_t)x[r].y;
+              par[src[r] * 64 + ((2 * lane) ^ src[r])] = (int32_t)x[r].x;
+              par[src[r] * 64 + ((2 * lane + 1) ^ src[r])] = (int32_t)x[r].y;
             }
           }
         }
       }
-      // each lane's level as bit slices (bit l of S[b] = bit b of lane l's
-      // level); the first kOutLevels levels >= 2 of a light vertex for its
-      // scan, any further ones (rare) through collect_levels below
-      uint64_t S[kSlices], reached = 0;
+      // a light vertex's records (pull rounds, then the scan pass), four
+      // records' loads in flight: sources into the thread's table, each
+      // lane's record index as three bit slices rq (the masks are disjoint)
+      uint64_t rq[3] = {0ull, 0ull, 0ull}, cov = 0;
+      for (int q0 = 0; q0 < np; q0 += 4) {
+        int32_t pu[4];
+        uint64_t pmk[4];
 #pragma unroll
-      for (int b = 0; b < kSlices; ++b) S[b] = 0;
-      int Ls[kOutLevels];
-      uint64_t Ms[kOutLevels];
-      int nl = 0;
-      uint64_t gtodo = 0, rest = 0;
-      int last = 1;
-#pragma unroll
-      for (int k = 0; k < kOutLevels; ++k) {
-        Ls[k] = 1;
-        Ms[k] = 0;
-      }
-      // a light vertex's first-hit records from the pull rounds
-      int32_t pu[kPairs];
-      uint64_t pmk[kPairs];
-      uint64_t covered = 0;
-#pragma unroll
-      for (int q = 0; q < kPairs; ++q) {
-        pu[q] = 0;
-        pmk[q] = 0;
-      }
-      if (valid && slot < 0) {
-        const int np = p.pair_n[v];
-#pragma unroll
-        for (int q = 0; q < kPairs; ++q) {
-          if (q < np) {
-            const int64_t at = (int64_t)q * p.n + v;
-            pu[q] = p.pair_u[at];
-            pmk[q] = p.pair_m[at * W + h];
-            covered |= pmk[q];
+        for (int r = 0; r < 4; ++r) {
+          pu[r] = 0;
+          pmk[r] = 0;
+          if (q0 + r < np) {
+            const int64_t at = (int64_t)(q0 + r) * p.n + v;
+            pu[r] = p.pair_u[at];
+            pmk[r] = p.pair_m[at * W + h];
           }
         }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+          if (q0 + r < np) my_pu[q0 + r] = pu[r];
+        const uint64_t all4 = pmk[0] | pmk[1] | pmk[2] | pmk[3];
+        cov |= all4;
+        rq[0] |= pmk[1] | pmk[3];
+        rq[1] |= pmk[2] | pmk[3];
+        if (q0 & 4) rq[2] |= all4;
       }
+      // each lane's level as bit slices: bit l of S[b] = bit b of lane l's level
+      uint64_t S[kSlices], reached = 0, m01[2] = {0ull, 0ull};
+#pragma unroll
+      for (int b = 0; b < kSlices; ++b) S[b] = 0;
       for (int L0 = 0; L0 < rounds; L0 += kPre) {  // uniform: the whole warp
         uint64_t pm[kPre];
 #pragma unroll
         for (int j = 0; j < kPre; ++j)
           pm[j] = valid && L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] : 0ull;
+        if (L0 == 0) {
+          m01[0] = pm[0];
+          m01[1] = pm[1];
+        }
+        // L0 is a multiple of kPre = 8: bits 0..2 of level L0 + j are those
+        // of j, known at compile time; bits 3.. those of L0, the same for the
+        // whole batch
+        uint64_t batch = 0;
 #pragma unroll
         for (int j = 0; j < kPre; ++j) {
           const uint64_t m = pm[j];
-          const int L = L0 + j;
           const unsigned c = __reduce_add_sync(kMsFull, (unsigned)__popcll(m));
-          if (lane == 0 && c) atomicAdd(&s_cnt[L], (unsigned long long)c);
-          reached |= m;
+          if (lane == 0 && c) atomicAdd(&s_cnt[L0 + j], c);
+          batch |= m;
 #pragma unroll
-          for (int b = 0; b < kSlices; ++b)
-            if ((L >> b) & 1) S[b] |= m;
-          const uint64_t scan = m & ~covered;
-          if (scan && L >= 2 && slot < 0) {
-            if (nl < kOutLevels) {
-#pragma unroll
-              for (int k = 0; k < kOutLevels; ++k)
-                if (k == nl) {
-                  Ls[k] = L;
-                  Ms[k] = scan;
-                }
-              ++nl;
-              gtodo |= scan;
-              last = L;
-            } else {
-              rest |= scan;
-            }
-          }
+          for (int b = 0; b < 3; ++b)
+            if ((j >> b) & 1) S[b] |= m;
         }
+        reached |= batch;
+#pragma unroll
+        for (int b = 3; b < kSlices; ++b)
+          if ((L0 >> b) & 1) S[b] |= batch;
       }
-      // light vertices: the whole in-list (<= kPullLight entries), kScanG
-      // entries' loads in flight, kOutLevels levels per pass.  The lanes of
-      // the first entry that hits (often most of them; all of them for an
-      // in-degree of one) are kept as a mask, not stored one by one.
-      int from = last + 1;
-      int32_t u_first = 0;
-      uint64_t m_first = 0;
-      bool first_pass = true;
-      while (gtodo) {
-        for (int64_t j0 = s; j0 < e && gtodo; j0 += kScanG) {
-          int32_t u[kScanG];
-          uint64_t b[kScanG];
-#pragma unroll
-          for (int k = 0; k < kScanG; ++k) u[k] = j0 + k < e ? __ldg(p.in_idx + j0 + k) : -1;
-#pragma unroll
-          for (int k = 0; k < kScanG; ++k)
-            b[k] = u[k] >= 0 ? parent_hits<W>(p, u[k], h, Ls, Ms, gtodo) : 0;
-#pragma unroll
-          for (int k = 0; k < kScanG; ++k) {
-            uint64_t bk = b[k] & gtodo;
-            gtodo &= ~bk;
-            if (bk && first_pass && !m_first) {
-              m_first = bk;
-              u_first = u[k];
-              bk = 0;
-            }
-            while (bk) {
-              const int bit = __ffsll((long long)bk) - 1;
-              bk &= bk - 1;
-              my_par[bit] = u[k];
-            }
-          }
-        }
-        first_pass = false;
-        gtodo = 0;
-        if (rest) {  // more than kOutLevels levels at this vertex
-          gtodo = collect_levels<W>(p, v, h, rounds, rest, from, Ls, Ms);
-          rest &= ~gtodo;
-          if (!gtodo) rest = 0;
-        }
-      }
-      // the largest first-hit mask (scan or pull record) is applied lane by
-      // lane below; the others go into the tile row now
-      int32_t d = u_first;
-      uint64_t dm = m_first;
-      {
-        int best = -1, bc = __popcll(m_first);
-#pragma unroll
-        for (int q = 0; q < kPairs; ++q) {
-          const int c = __popcll(pmk[q]);
-          if (c > bc) {
-            bc = c;
-            best = q;
-          }
-        }
-        if (best >= 0) {
-          for (uint64_t x = m_first; x; x &= x - 1) my_par[__ffsll((long long)x) - 1] = u_first;
-#pragma unroll
-          for (int q = 0; q < kPairs; ++q)
-            if (q == best) {
-              d = pu[q];
-              dm = pmk[q];
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < kPairs; ++q)
-          if (q != best)
-            for (uint64_t x = pmk[q]; x; x &= x - 1) my_par[__ffsll((long long)x) - 1] = pu[q];
+      __syncwarp();  // the candidate rows copied by the warp are in place
+      // levels 0 and 1 (rare): the vertex itself, the lane's root
+      for (uint64_t x = m01[0]; x; x &= x - 1) my_row[(__ffsll((long long)x) - 1) ^ lane] = (int32_t)v;
+      for (uint64_t x = m01[1]; x; x &= x - 1) {
+        const int b = __ffsll((long long)x) - 1;
+        my_row[b ^ lane] = p.roots[64 * h + b];
       }
       __syncwarp();
-      // rows: lane l of this half, vertices tile*32 .. tile*32 + 31; four
-      // lanes' levels built at a time as the bytes of a word (0xFF unreached)
+      // rows: lane l of this half, vertices tile*32 .. tile*32 + 31, a 32-lane
+      // word of the masks at a time; four lanes' levels are built as the
+      // bytes of a word (0xFF unreached, which sign-extends to -1)
       const int lanes = min(64, p.k - 64 * h);
-      int nsl = 1;
-      while (nsl < kSlices && (rounds - 1) >> nsl) ++nsl;
-      int32_t *out_l = p.levels + (int64_t)(64 * h) * p.n + v;
-      int32_t *out_p = p.parents + (int64_t)(64 * h) * p.n + v;
-      for (int l4 = 0; l4 < lanes; l4 += 4) {
-        uint32_t word = spread4(~(uint32_t)(reached >> l4) & 0xFu) * 0xFFu;
+      int32_t *base_l = p.levels + v;
+      int32_t *base_p = p.parents + v;
+#pragma unroll 1
+      for (int hw = 0; hw < 2 && 32 * hw < lanes; ++hw) {
+        uint32_t sl[kSlices];
 #pragma unroll
-        for (int b = 0; b < kSlices; ++b)
-          if (b < nsl) word |= spread4((uint32_t)(S[b] >> l4) & 0xFu) << b;
-        const uint32_t dq = (uint32_t)(dm >> l4);
+        for (int b = 0; b < kSlices; ++b) sl[b] = (uint32_t)(S[b] >> (32 * hw));
+        const uint32_t rw = (uint32_t)(reached >> (32 * hw));
+        const uint32_t cw = (uint32_t)(cov >> (32 * hw));
+        uint32_t qs[3];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int l = l4 + i;
-          if (l < lanes) {
-            const uint32_t lv = (word >> (8 * i)) & 0xFFu;
-            int32_t pv = (dq >> i) & 1u ? d : my_par[l];
-            if (lv == 1) pv = p.roots[64 * h + l];
-            if (lv == 0) pv = (int32_t)v;
-            if (valid) {
-              *out_l = lv == 0xFFu ? -1 : (int32_t)lv;
-              *out_p = lv == 0xFFu ? -1 : pv;
+        for (int b = 0; b < 3; ++b) qs[b] = (uint32_t)(rq[b] >> (32 * hw));
+        const int lend = min(32, lanes - 32 * hw);
+        auto group = [&](int l4, auto checked) {
+          uint32_t word = spread4(~(rw >> l4) & 0xFu) * 0xFFu;
+#pragma unroll
+          for (int b = 0; b < kSlices; ++b)
+            if (b < nsl) word |= spread4((sl[b] >> l4) & 0xFu) << b;
+          // four lanes' record indices, bytes of a word as the levels
+          const uint32_t qw = spread4((qs[0] >> l4) & 0xFu) | (spread4((qs[1] >> l4) & 0xFu) << 1) |
+                              (spread4((qs[2] >> l4) & 0xFu) << 2);
+          const uint32_t cq = cw >> l4;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            if (!decltype(checked)::value || l4 + i < lend) {
+              const int l = 32 * hw + l4 + i;
+              const int32_t lv = (int32_t)(int8_t)(uint8_t)(word >> (8 * i));
+              const int32_t pv =
+                  (cq >> i) & 1u ? my_pu[(qw >> (8 * i)) & 0xFFu] : my_row[l ^ lane];
+              const int64_t row = (int64_t)(64 * h + l) * p.n;
+              if (valid) {
+                base_l[row] = lv;
+                base_p[row] = lv < 0 ? -1 : pv;
+              }
             }
-            out_l += p.n;
-            out_p += p.n;
           }
+        };
+        if (lend == 32) {
+          for (int l4 = 0; l4 < 32; l4 += 4) group(l4, Flag<false>{});
+        } else {
+          for (int l4 = 0; l4 < lend; l4 += 4) group(l4, Flag<true>{});
         }
       }
       __syncwarp();
@@ -1072,7 +1173,7 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   // round ended
   __syncthreads();
   for (int i = threadIdx.x; i < rounds; i += blockDim.x) {
-    const unsigned long long c = s_cnt[i];
+    const unsigned long long c = s_cnt[i];  // widened for the global sums
     if (!c) continue;
     atomicAdd(reinterpret_cast<unsigned long long *>(&p.stats->visited), c);
     if (i >= 1)
@@ -1111,6 +1212,13 @@ int ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   CG_CUDA(cudaLaunchKernelEx(&cfg, msbfs_ledger<W>, p));
+  int scan_per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&scan_per_sm, msbfs_scan<W>, kScanBlock, 0));
+  if (scan_per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+  const int64_t chunks = ((g->n + 31) / 32 + kScanWords - 1) / kScanWords;
+  int64_t scan_blocks = (chunks + kScanBlock / 32 - 1) / (kScanBlock / 32);
+  if (scan_blocks > (int64_t)scan_per_sm * g->num_sms) scan_blocks = (int64_t)scan_per_sm * g->num_sms;
+  msbfs_scan<W><<<(unsigned)scan_blocks, kScanBlock, 0, g->stream>>>(p);
   const int smem = kOutWarps * kOutWarpBytes;
   CG_CUDA(cudaFuncSetAttribute(msbfs_outputs<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                smem));
@@ -1123,6 +1231,7 @@ int ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d
   const int64_t cap = (int64_t)out_per_sm * g->num_sms;
   if (blocks > cap) blocks = cap;
   msbfs_outputs<W><<<(unsigned)blocks, kOutBlock, smem, g->stream>>>(p);
+  msbfs_fixup<W><<<(unsigned)g->num_sms, kScanBlock, 0, g->stream>>>(p);
   CG_CUDA(cudaGetLastError());
   return CG_OK;
 }

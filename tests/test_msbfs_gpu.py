@@ -183,3 +183,32 @@ def test_msbfs_history_overflow_in_a_captured_graph(built_lib, oracle_mod):
       assert g.last_stats()["status"] == 0
       assert np.array_equal(d_lv.cpu().numpy(), wl) and np.array_equal(d_pa.cpu().numpy(), wp)
       exe.close()
+
+
+@pytest.mark.parametrize("lane_words", [1, 2])
+@pytest.mark.parametrize("direction", MS_DIRS)
+def test_msbfs_more_parents_than_records(built_lib, oracle_mod, lane_words, direction):
+  """Light vertices with more distinct parents across lanes than they have
+  (source, lanes) records: 128 roots hang off 24 middle vertices, and two
+  targets of in-degree 24 see a different parent in almost every lane, so
+  their records run out and the fix-up pass writes the rest."""
+  roots = list(range(128))
+  mid = [128 + j for j in range(24)]
+  t1, t2 = 152, 153
+  src, dst = [], []
+  for r in roots:
+    src.append(r)
+    dst.append(mid[r % 24])
+  for m in mid:
+    src += [m, m]
+    dst += [t1, t2]
+  src += [t1, 154, 155]
+  dst += [154, 155, 156]
+  a = preprocess.from_edges(157, np.array(src), np.array(dst), symmetrize=True)
+  k = 64 * lane_words
+  rl, rp, _ = _oracle_all(oracle_mod, a, roots[:k])
+  with Graph(a) as g:
+    g.set_options(lane_words=lane_words, direction=direction)
+    lv, pa, st = g.msbfs(roots[:k])
+    assert st["status"] == 0
+    assert np.array_equal(lv, rl) and np.array_equal(pa, rp)
