@@ -36,6 +36,7 @@ static void free_graph(cg_graph *g) {
   cudaFree(g->in_off);
   cudaFree(g->in_idx);
   cudaFree(g->bitmaps);
+  cudaFree(g->dead);
   cudaFree(g->queue);
   cudaFree(g->bigoff);
   cudaFree(g->ctl);

@@ -272,7 +272,7 @@ __device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nx
   const int lane = lane_id();
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int64_t w = warp_id_global(); w < p.words; w += nwarps) {
-    const uint32_t seen = p.vis[w] | cur[w];
+    const uint32_t seen = p.vis[w] | cur[w] | (p.dead ? p.dead[w] : 0u);
     const int64_t v = w * 32 + lane;
     const bool active = v < p.n && !((seen >> lane) & 1u);
     if (__ballot_sync(kFull, active) == 0) continue;
@@ -639,8 +639,47 @@ int64_t bfs_big_capacity(int64_t n, int64_t nnz) {
   return c < n ? c : n;
 }
 
+// Bit v of dead[v / 32]: vertex v has no in-edges, so no round reaches it
+// (bits past n are set too).
+__global__ void dead_map_kernel(int64_t n, int64_t words, const int64_t *__restrict__ in_off,
+                                uint32_t *dead) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    int64_t prev = w * 32 < n ? in_off[w * 32] : 0;
+    for (int b = 0; b < 32; ++b) {
+      const int64_t v = w * 32 + b;
+      if (v >= n) {
+        m |= 1u << b;
+        continue;
+      }
+      const int64_t next = in_off[v + 1];
+      if (next == prev) m |= 1u << b;
+      prev = next;
+    }
+    dead[w] = m;
+  }
+}
+
+int dead_prepare(cg_graph *g) {
+  if (g->dead) return CG_OK;
+  const int64_t words = (g->n + 31) / 32;
+  if (cudaMalloc(&g->dead, sizeof(uint32_t) * (size_t)words) != cudaSuccess) {
+    g->dead = nullptr;
+    return CG_ERR_OUT_OF_MEMORY;
+  }
+  g->device_bytes += sizeof(uint32_t) * words;
+  const int64_t blocks = (words + 255) / 256;
+  dead_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, g->stream>>>(
+      g->n, words, g->in_off, g->dead);
+  CG_CUDA(cudaGetLastError());
+  return CG_OK;
+}
+
 int bfs_prepare(cg_graph *g) {
   if (g->bitmaps) return CG_OK;
+  int rc = dead_prepare(g);
+  if (rc) return rc;
   int dev_coop = 0;
   CG_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, g->device));
   if (!dev_coop) return CG_ERR_NOT_SUPPORTED;
@@ -691,6 +730,7 @@ int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents,
   p.fr0 = g->bitmaps + g->words;
   p.fr1 = g->bitmaps + 2 * g->words;
   p.fr2 = g->bitmaps + 3 * g->words;
+  p.dead = g->dead;
   p.queue0 = g->queue;
   p.queue1 = g->queue + g->n;
   p.bigoff0 = g->bigoff;

@@ -90,6 +90,7 @@ struct BfsParams {
   const int64_t *__restrict__ out_off;
   const int32_t *__restrict__ out_idx;
   uint32_t *vis, *fr0, *fr1, *fr2;
+  const uint32_t *dead;  // vertices without in-edges (never reached), or null
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   int32_t *levels, *parents;
@@ -123,6 +124,7 @@ struct cg_graph {
   // per-root search state
   int64_t words = 0;
   uint32_t *bitmaps = nullptr;  // vis | fr0 | fr1 | fr2, 4 * words
+  uint32_t *dead = nullptr;     // 1 bit per vertex: no in-edges (dead_prepare)
   int32_t *queue = nullptr;     // 2 * n
   uint32_t *bigoff = nullptr;   // 2 * bcap
   int64_t bcap = 0;
@@ -148,6 +150,7 @@ namespace cg {
 // Records a CUDA error for cg_last_error_string and returns CG_ERR_CUDA.
 int cuda_fail(cudaError_t e, const char *what);
 int bfs_prepare(cg_graph *g);
+int dead_prepare(cg_graph *g);
 int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems);
 void msbfs_release(cg_graph *g);
 }  // namespace cg

@@ -66,6 +66,7 @@ struct MsParams {
   uint64_t *vis, *fr0, *fr1, *fr2;
   uint32_t *touched0, *touched1, *touched2;
   uint32_t *scanmap;  // light vertices with lanes their records leave open (ledger)
+  const uint32_t *dead;  // vertices without in-edges (never reached after round 0)
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
@@ -597,6 +598,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.pair_n = s->pair_n;
   p.touched0 = s->touched;
   p.scanmap = s->touched + 3 * p.words;
+  p.dead = g->dead;
   p.touched1 = s->touched + p.words;
   p.touched2 = s->touched + 2 * p.words;
   p.queue0 = s->queue;

@@ -839,6 +839,8 @@ static int ms_history_planes(const cg_graph *g, int lane_words) {
 }
 
 static int ms_alloc_state(cg_graph *g, int lane_words) {
+  int rc0 = dead_prepare(g);
+  if (rc0) return rc0;
   MsState *old = reinterpret_cast<MsState *>(g->ms_ctl);
   if (old && g->ms_lane_words == lane_words && old->hist_opt == g->opt.ms_history) return CG_OK;
   ms_free_state(old);

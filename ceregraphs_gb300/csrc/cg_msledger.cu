@@ -265,7 +265,11 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         const int64_t v = base + lane;
         Mask<W> want = Mask<W>::zero();
         int64_t s = 0, e = 0;
-        if (v < p.n) {
+        // after round 0 a vertex without in-edges is in no frontier and wants
+        // nothing it could find (round 0 may still hold such a root)
+        const uint32_t dw = L > 0 && p.dead ? __ldg(p.dead + (base >> 5)) : 0u;
+        if (dw == kMsFull) continue;
+        if (v < p.n && !((dw >> lane) & 1u)) {
           const Mask<W> fv = ld_mask<W>(cur, v);
           const Mask<W> seen = ld_mask<W>(p.vis, v) | fv;
           if (fv.any()) st_mask<W>(p.vis, v, seen);

@@ -114,6 +114,7 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   p.fr0 = bitmaps + words;
   p.fr1 = bitmaps + 2 * words;
   p.fr2 = bitmaps + 3 * words;
+  p.dead = nullptr;  // no per-graph state here: every vertex is scanned
   int32_t *queue = reinterpret_cast<int32_t *>(base + kOffQueue);
   p.queue0 = queue;
   p.queue1 = queue + n;
