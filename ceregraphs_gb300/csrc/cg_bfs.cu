@@ -545,10 +545,14 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
       R0->big = (1ull << 32) | (unsigned long long)deg;
     }
   }
+  // the sync word's generation, read before this block's first arrival (it
+  // cannot advance before then); every completed wait adds one
+  unsigned gen = 0;
+  if (threadIdx.x == 0) gen = (unsigned)ld_acquire64(&ctl->wait.sync);
   __syncthreads();
   if (threadIdx.x == 0)
-    s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns,
-                                p.unmatched_wait ? 1u : 0u, SetupDecision{ctl, p.stats});
+    s_payload = arrive_and_wait_gen(&ctl->wait, gen++, &ctl->status, p.timeout_ns,
+                                    p.unmatched_wait ? 1u : 0u, SetupDecision{ctl, p.stats});
   __syncthreads();
   bool ok = s_payload != kWaitFailed;
 
@@ -585,8 +589,8 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
       if (a) atomicAdd(&Rn->nf[sh], a);
       if (b) atomicAdd(&Rn->mf[sh], b);
       if (c) atomicAdd(&Rn->visdeg[sh], c);
-      s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
-                                  RoundDecision{&p, L, dir});
+      s_payload = arrive_and_wait_gen(&ctl->wait, gen++, &ctl->status, p.timeout_ns, 0u,
+                                      RoundDecision{&p, L, dir});
     }
     __syncthreads();
     const unsigned payload = s_payload;

@@ -206,12 +206,13 @@ constexpr unsigned kWaitFailed = 0xffffffffu;
 // kWaitFailed, so a wait that can never complete ends the kernel instead of
 // spinning.  `extra` > 0 makes the top counter expect that many arrivals that
 // never come (the test hook behind cg_options.test_unmatched_wait).
+// arrive_and_wait for a caller that knows the generation g of the sync word
+// (the value before this wait; each completed wait adds one), saving the load
+// of it from the arrival's critical path.
 template <class Decide>
-__device__ __forceinline__ unsigned arrive_and_wait(GridWait *w, int *status,
-                                                    long long timeout_ns, unsigned extra,
-                                                    Decide decide) {
-  const unsigned long long s0 = ld_acquire64(&w->sync);
-  const unsigned g = (unsigned)s0;
+__device__ __forceinline__ unsigned arrive_and_wait_gen(GridWait *w, unsigned g, int *status,
+                                                        long long timeout_ns, unsigned extra,
+                                                        Decide decide) {
   const unsigned groups = gridDim.x < (unsigned)kWaitGroups ? gridDim.x : kWaitGroups;
   const unsigned grp = blockIdx.x % kWaitGroups;
   const unsigned members = (gridDim.x - grp + kWaitGroups - 1) / kWaitGroups;
@@ -239,6 +240,14 @@ __device__ __forceinline__ unsigned arrive_and_wait(GridWait *w, int *status,
       }
     }
   }
+}
+
+template <class Decide>
+__device__ __forceinline__ unsigned arrive_and_wait(GridWait *w, int *status,
+                                                    long long timeout_ns, unsigned extra,
+                                                    Decide decide) {
+  const unsigned g = (unsigned)ld_acquire64(&w->sync);
+  return arrive_and_wait_gen(w, g, status, timeout_ns, extra, decide);
 }
 
 struct NoDecision {
