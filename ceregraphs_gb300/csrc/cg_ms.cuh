@@ -49,6 +49,7 @@ struct MsCtl {
   int switches;
   unsigned exited;                // blocks past the final pass (finish time)
   unsigned nover;                 // light vertices whose records ran out (scan pass)
+  unsigned scan_work;             // scan pass: chunks of scanmap handed out
   unsigned long long visited;
   unsigned long long done[2];     // lanes whose search ended (cleared by the host)
   long long t_start;

@@ -803,7 +803,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
 // ---- scan pass, output pass, fix-up pass ------------------------------------
 
 constexpr int kScanBlock = 256;  // scan and fix-up passes: threads a block
-constexpr int kScanWords = 8;    // scan pass: scanmap words a warp takes at a time
+constexpr int kScanWords = 4;    // scan pass: scanmap words a warp takes at a time
 constexpr int kScanG = 4;        // in-list entries loaded together
 constexpr int kPre = 8;          // history planes loaded together (the output pass needs 8)
 
@@ -833,7 +833,7 @@ __device__ __forceinline__ uint64_t parent_hits(const MsParams &p, int32_t u, in
 // lane in F_{level - 1}[u] is the lane's parent, the lowest-index rule.  One
 // pass over the list resolves up to kOutLevels levels; hit(u, lanes) gets
 // each entry that resolves lanes.
-template <int W, class Hit>
+template <int W, int G, class Hit>
 __device__ __forceinline__ void scan_in_list(const MsParams &p, int64_t v, int h, int rounds,
                                              int64_t s, int64_t e, uint64_t todo, Hit &&hit) {
   int L = 2;
@@ -873,16 +873,16 @@ __device__ __forceinline__ void scan_in_list(const MsParams &p, int64_t v, int h
       }
       L += taken;
     }
-    for (int64_t j0 = s; j0 < e && gtodo; j0 += kScanG) {
-      int32_t u[kScanG];
-      uint64_t b[kScanG];
+    for (int64_t j0 = s; j0 < e && gtodo; j0 += G) {
+      int32_t u[G];
+      uint64_t b[G];
 #pragma unroll
-      for (int k = 0; k < kScanG; ++k) u[k] = j0 + k < e ? __ldg(p.in_idx + j0 + k) : -1;
+      for (int k = 0; k < G; ++k) u[k] = j0 + k < e ? __ldg(p.in_idx + j0 + k) : -1;
 #pragma unroll
-      for (int k = 0; k < kScanG; ++k)
+      for (int k = 0; k < G; ++k)
         b[k] = u[k] >= 0 ? parent_hits<W>(p, u[k], h, Ls, Ms, gtodo) : 0;
 #pragma unroll
-      for (int k = 0; k < kScanG; ++k) {
+      for (int k = 0; k < G; ++k) {
         const uint64_t bk = b[k] & gtodo;
         if (bk) {
           gtodo &= ~bk;
@@ -907,8 +907,9 @@ __device__ __forceinline__ uint64_t records_mask(const MsParams &p, int64_t v, i
 // (in-degree 1 .. kPullLight; heavier ones have candidate slots) that the
 // rounds marked in scanmap: reached by a push round at a level >= 2, or with
 // more pull-round first hits than records.  A warp takes kScanWords words of
-// the map, compacts their marked vertices in shared memory, and gives each
-// thread one.
+// the map at a time (the first by its index, the next from a counter, claimed
+// before the current chunk is worked), compacts their marked vertices in
+// shared memory, and gives each thread one.
 // The lanes a vertex's records leave open are resolved by scan_in_list and
 // appended as records; a vertex that runs out of records goes on a list
 // (queue0, free once the rounds are over) for the fix-up pass.
@@ -920,8 +921,13 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
   if (rounds <= 2) return;
   const int lane = lane_id();
   int32_t *list = s_list[threadIdx.x >> 5];
-  const int64_t nwarps = (int64_t)gridDim.x * (kScanBlock / 32);
-  for (int64_t w0 = warp_id_global() * kScanWords; w0 < p.words; w0 += nwarps * kScanWords) {
+  const unsigned nwarps = gridDim.x * (kScanBlock / 32);
+  const unsigned nchunks = (unsigned)((p.words + kScanWords - 1) / kScanWords);
+  unsigned chunk = (unsigned)warp_id_global();
+  while (chunk < nchunks) {
+    unsigned next = 0;
+    if (lane == 0) next = nwarps + atomicAdd(&p.ctl->scan_work, 1u);
+    const int64_t w0 = (int64_t)chunk * kScanWords;
     const int64_t wi = w0 + lane;
     uint32_t bits = lane < kScanWords && wi < p.words ? p.scanmap[wi] : 0u;
     const int c = __popc(bits);
@@ -943,7 +949,7 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
       bool over = false;
       for (int h = 0; h < W && 64 * h < p.k; ++h) {
         const uint64_t covered = records_mask<W>(p, v, h, np0);
-        scan_in_list<W>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
+        scan_in_list<W, kScanG>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
           if (np < kRecords) {
             const int64_t at = (int64_t)np * p.n + v;
             p.pair_u[at] = u;
@@ -959,6 +965,7 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
       if (over) p.queue0[atomicAdd(&p.ctl->nover, 1u)] = (int32_t)v;
     }
     __syncwarp();
+    chunk = __shfl_sync(kMsFull, next, 0);
   }
 }
 
@@ -978,7 +985,8 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_fixup(MsParams p) {
     const int np = p.pair_n[v];
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
       const uint64_t covered = records_mask<W>(p, v, h, np);
-      scan_in_list<W>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
+      // the whole (<= kPullLight) in-list's loads in flight at once
+      scan_in_list<W, kPullLight>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
         for (uint64_t x = m; x; x &= x - 1)
           p.parents[(int64_t)(64 * h + __ffsll((long long)x) - 1) * p.n + v] = u;
       });
