@@ -177,6 +177,39 @@ def min_parents(A_csr, levels, source):
   return parent.astype(np.int32)
 
 
+def fifo_parents(in_off, in_idx, levels, source):
+  """Parents by the rule of the reference's own host BFS, scipy
+  breadth_first_order on A^T (run_graph500.py:383-395, run_bfs.py:517-527):
+  it pops its queue in order and hands each not-yet-seen out-neighbour (in
+  ascending id order) the popped vertex as predecessor.  So the parent of a
+  vertex at level L+1 is its level-L in-neighbour of smallest queue rank, and
+  level L+1 is queued in order of (rank of the parent, vertex id).  Restated
+  level by level from the levels alone, without scipy.  in_off/in_idx: the
+  in-lists (row r of A: the sources of the edges into r)."""
+  n = len(levels)
+  levels = np.asarray(levels, dtype=np.int64)
+  in_off = np.asarray(in_off, dtype=np.int64)
+  dst = np.repeat(np.arange(n, dtype=np.int64), np.diff(in_off))
+  src = np.asarray(in_idx, dtype=np.int64)
+  parent = np.full(n, -1, dtype=np.int64)
+  rank = np.full(n, -1, dtype=np.int64)
+  parent[source] = source
+  rank[source] = 0
+  big = np.iinfo(np.int64).max
+  for L in range(int(levels.max())):
+    sel = (levels[dst] == L + 1) & (levels[src] == L)
+    best = np.full(n, big, dtype=np.int64)
+    np.minimum.at(best, dst[sel], rank[src[sel]] * n + src[sel])
+    vs = np.nonzero(levels == L + 1)[0]
+    if not len(vs):
+      break
+    parent[vs] = best[vs] % n
+    prank = best[vs] // n
+    order = np.lexsort((vs, prank))
+    rank[vs[order]] = np.arange(len(vs))
+  return parent.astype(np.int32)
+
+
 def graph500_validate(A_csr, source, levels, parent):
   """The five Graph500 tree checks, stated in our own words:
 

@@ -15,7 +15,8 @@ imported unmodified:
 * bfs/plots/bfs_tree_plot.py:140        invalid_parents()
 * bfs/implementation/graph_loader.py:27 load_graph()          -> (dst, src) rule
 * scipy.sparse.csgraph.breadth_first_order on A^T, as run_graph500.py:383-395
-  calls it, for levels (derived from its predecessors) and reached sets.
+  calls it, for levels (derived from its predecessors), reached sets and its
+  own predecessors (the FIFO parent rule).
 
 The lowest-index parents stored next to the levels are derived from those
 levels with np.minimum.at over the edge list (bfs/README.md:208-224), i.e.
@@ -122,10 +123,12 @@ def search_record(A, source, is_symmetric, bfs_timing, device_io, bfs_tree_plot,
   m, conv, _, _ = bfs_timing.compute_m_and_gteps(A.tocoo(), visited, is_symmetric, 875e6)
   rec = {"source": int(source), "rounds": int(lv.max()) + 1, "visited": int(visited.sum()),
          "m": int(m), "m_convention": conv, "levels_sha": sha(lv), "parents_sha": sha(mp),
+         "scipy_parents_sha": sha(pred.astype(np.int32)),
          "scipy_parent_differs": int(np.sum((pred != mp) & (lv > 0)))}
   if full:
     rec["levels"] = lv
     rec["parents"] = mp
+    rec["scipy_parents"] = pred.astype(np.int32)
   return rec
 
 
@@ -221,6 +224,7 @@ def main(ref):
       rec = search_record(A, r, True, bfs_timing, device_io, bfs_tree_plot, full=True)
       arrays[f"{key}_r{r}_levels"] = rec.pop("levels")
       arrays[f"{key}_r{r}_parents"] = rec.pop("parents")
+      arrays[f"{key}_r{r}_scipy_parents"] = rec.pop("scipy_parents")
       recs.append(rec)
     out["searches"][key] = recs
   for key, roots in (("s16_e16_seed0", [0] + out["pick_sources"]["s16_e16_seed0_k64_seed1"][:3]),):
@@ -249,6 +253,7 @@ def main(ref):
     rec = search_record(D, r, False, bfs_timing, device_io, bfs_tree_plot, full=True)
     arrays[f"dir600_r{r}_levels"] = rec.pop("levels")
     arrays[f"dir600_r{r}_parents"] = rec.pop("parents")
+    arrays[f"dir600_r{r}_scipy_parents"] = rec.pop("scipy_parents")
     recs.append(rec)
   out["searches"]["dir600"] = recs
 

@@ -129,3 +129,28 @@ def test_validator_rejects_wrong_levels(oracle_mod):
   l2, p2, rounds = oracle_mod.bfs_csr(A, iso)
   assert rounds == 1 and (l2 >= 0).sum() == 1 and p2[iso] == iso
   assert oracle_mod.graph500_validate(sparse.csr_matrix(A), iso, l2, p2) == []
+
+
+def test_oracle_fifo_parents_match_scipy(oracle_mod):
+  """The oracle's restatement of scipy's predecessor (FIFO) rule gives the
+  reference's own breadth_first_order parents, on R-MAT and on the directed
+  matrix with self-loops."""
+  for key in ("s10_e16_seed0", "s12_e16_seed0", "s12_e4_seed0"):
+    A = _graph(oracle_mod, key)
+    for rec in G["searches"][key]:
+      r = rec["source"]
+      lv = ARR[f"{key}_r{r}_levels"]
+      fp = oracle_mod.fifo_parents(A.indptr, A.indices, lv, r)
+      assert np.array_equal(fp, ARR[f"{key}_r{r}_scipy_parents"]), (key, r)
+      assert sha(fp) == rec["scipy_parents_sha"]
+  A = _graph(oracle_mod, "s16_e16_seed0")
+  for rec in G["searches"]["s16_e16_seed0"]:
+    lv, _, _ = oracle_mod.bfs_csr(A, rec["source"])
+    assert sha(oracle_mod.fifo_parents(A.indptr, A.indices, lv, rec["source"])) == \
+        rec["scipy_parents_sha"]
+  D = csr_from(ARR["dir600_indptr"], ARR["dir600_indices"], 600)
+  for rec in G["searches"]["dir600"]:
+    r = rec["source"]
+    fp = oracle_mod.fifo_parents(D.indptr, D.indices, ARR[f"dir600_r{r}_levels"], r)
+    assert np.array_equal(fp, ARR[f"dir600_r{r}_scipy_parents"])
+    assert oracle_mod.graph500_validate(D, r, ARR[f"dir600_r{r}_levels"], fp) == []
