@@ -33,6 +33,8 @@ CG_DIR_AUTO = 0
 CG_DIR_TOPDOWN = 1
 CG_DIR_BOTTOMUP = 2
 CG_DIR_TAU = 3
+CG_PARENT_LOWEST = 0  # lowest-index in-neighbour one level up (bfs/README.md:208-224)
+CG_PARENT_FIFO = 1    # scipy breadth_first_order's predecessor (run_graph500.py:383-395)
 
 CG_GRAPH_DEVICE_PTRS = 1
 CG_GRAPH_SYMMETRIC = 2
@@ -46,7 +48,8 @@ class CgOptions(ctypes.Structure):
               ("block_size", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
               ("level_cap", ctypes.c_int32), ("wait_timeout_ms", ctypes.c_int32),
               ("lane_words", ctypes.c_int32), ("ms_alpha", ctypes.c_float),
-              ("test_unmatched_wait", ctypes.c_int32), ("ms_history", ctypes.c_int32)]
+              ("test_unmatched_wait", ctypes.c_int32), ("ms_history", ctypes.c_int32),
+              ("parent_rule", ctypes.c_int32)]
 
   def as_dict(self):
     return {k: getattr(self, k) for k, _ in self._fields_}

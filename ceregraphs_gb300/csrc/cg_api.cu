@@ -31,6 +31,7 @@ static void free_graph(cg_graph *g) {
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
   msbfs_release(g);
+  fifo_free(g->fifo);
   if (g->out_off && g->out_off != g->in_off) cudaFree(g->out_off);
   if (g->out_idx && g->out_idx != g->in_idx) cudaFree(g->out_idx);
   cudaFree(g->in_off);
@@ -187,6 +188,8 @@ int cg_graph_set_options(cg_graph *g, const cg_options *opt) {
   if (opt->block_size < 0 || (opt->block_size % 32) != 0 || opt->block_size > 512)
     return CG_ERR_INVALID_ARG;
   if (opt->lane_words != 1 && opt->lane_words != 2) return CG_ERR_INVALID_ARG;
+  if (opt->parent_rule != CG_PARENT_LOWEST && opt->parent_rule != CG_PARENT_FIFO)
+    return CG_ERR_INVALID_ARG;
   if (opt->alpha < 0 || opt->beta < 0 || opt->ms_alpha < 0 || opt->level_cap < 0 ||
       opt->wait_timeout_ms < 0)
     return CG_ERR_INVALID_ARG;
@@ -215,7 +218,9 @@ void *cg_graph_stream(const cg_graph *g) { return g ? (void *)g->stream : nullpt
 
 int cg_bfs_device(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents) {
   if (!g || !d_levels || !d_parents || root < 0 || root >= g->n) return CG_ERR_INVALID_ARG;
-  return bfs_launch(g, root, d_levels, d_parents);
+  const int rc = bfs_launch(g, root, d_levels, d_parents);
+  if (rc || g->opt.parent_rule != CG_PARENT_FIFO) return rc;
+  return fifo_parents(g, root, d_levels, d_parents);
 }
 
 int cg_graph_last_stats(cg_graph *g, cg_stats *stats) {
@@ -255,10 +260,12 @@ int cg_bfs(cg_graph *g, int64_t root, int32_t *levels, int32_t *parents, cg_stat
   }
   // page-locked outputs are written by the search kernel itself at its end
   // (the GPU's own SMs over the host link); pageable ones by a copy after it
-  int32_t *hl = pinned_device_ptr(levels), *hp = pinned_device_ptr(parents);
+  const bool fifo = g->opt.parent_rule == CG_PARENT_FIFO;
+  int32_t *hl = pinned_device_ptr(levels), *hp = fifo ? nullptr : pinned_device_ptr(parents);
   CG_CUDA(cudaEventRecord(g->ev0, g->stream));
   int rc = bfs_launch(g, root, g->tmp_levels, g->tmp_parents, hl, hp);
   if (rc) return rc;
+  if (fifo && (rc = fifo_parents(g, root, g->tmp_levels, g->tmp_parents))) return rc;
   CG_CUDA(cudaEventRecord(g->ev1, g->stream));
   const size_t bytes = sizeof(int32_t) * (size_t)g->n;
   if (levels && !hl)
@@ -276,12 +283,36 @@ int cg_bfs(cg_graph *g, int64_t root, int32_t *levels, int32_t *parents, cg_stat
   return local.status;
 }
 
+// FIFO parents for each of k finished searches (rows of k x n outputs); a
+// search that failed on the device keeps its status for the caller.
+static int fifo_all(cg_graph *g, const int64_t *roots, int32_t k, const int32_t *d_levels,
+                    int32_t *d_parents) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CG_CUDA(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) {
+    set_error_text("the FIFO parent rule synchronises with the stream: not capturable");
+    return CG_ERR_NOT_SUPPORTED;
+  }
+  cg_stats st;
+  CG_CUDA(cudaMemcpyAsync(&st, g->d_stats, sizeof(cg_stats), cudaMemcpyDeviceToHost, g->stream));
+  CG_CUDA(cudaStreamSynchronize(g->stream));
+  if (st.status) return CG_OK;
+  for (int32_t i = 0; i < k; ++i) {
+    const int rc = fifo_parents(g, roots[i], d_levels + (int64_t)i * g->n,
+                                d_parents + (int64_t)i * g->n);
+    if (rc) return rc;
+  }
+  return CG_OK;
+}
+
 int cg_msbfs_device(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels,
                     int32_t *d_parents) {
   if (!g || !roots || k <= 0 || !d_levels || !d_parents) return CG_ERR_INVALID_ARG;
   for (int32_t i = 0; i < k; ++i)
     if (roots[i] < 0 || roots[i] >= g->n) return CG_ERR_INVALID_ARG;
-  return msbfs_launch(g, roots, k, d_levels, d_parents);
+  int rc = msbfs_launch(g, roots, k, d_levels, d_parents);
+  if (rc || g->opt.parent_rule != CG_PARENT_FIFO) return rc;
+  return fifo_all(g, roots, k, d_levels, d_parents);
 }
 
 int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int32_t *parents,
@@ -295,6 +326,9 @@ int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int3
   CG_CUDA(cudaEventRecord(g->ev0, g->stream));
   rc = msbfs_launch(g, roots, k, g->ms_levels, g->ms_parents);
   if (rc) return rc;
+  if (g->opt.parent_rule == CG_PARENT_FIFO &&
+      (rc = fifo_all(g, roots, k, g->ms_levels, g->ms_parents)))
+    return rc;
   CG_CUDA(cudaEventRecord(g->ev1, g->stream));
   const size_t bytes = sizeof(int32_t) * (size_t)elems;
   if (levels)

@@ -110,6 +110,10 @@ struct BfsParams {
 
 }  // namespace cg
 
+namespace cg {
+struct FifoState;
+}
+
 struct cg_graph {
   int device = 0;
   int num_sms = 0;
@@ -144,15 +148,22 @@ struct cg_graph {
   int64_t device_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cg_stats *h_stats = nullptr;     // page-locked copy target of d_stats
+  cg::FifoState *fifo = nullptr;   // FIFO parent pass scratch (first use)
 };
 
 namespace cg {
 // Records a CUDA error for cg_last_error_string and returns CG_ERR_CUDA.
 int cuda_fail(cudaError_t e, const char *what);
+// Sets the text cg_last_error_string returns (a reason, not a CUDA error).
+void set_error_text(const char *text);
 int bfs_prepare(cg_graph *g);
 int dead_prepare(cg_graph *g);
 int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems);
 void msbfs_release(cg_graph *g);
+// Rewrites the parents of a finished search (d_levels final) by the FIFO rule
+// of scipy's breadth_first_order; synchronises with the handle's stream.
+int fifo_parents(cg_graph *g, int64_t root, const int32_t *d_levels, int32_t *d_parents);
+void fifo_free(FifoState *f);
 }  // namespace cg
 
 #define CG_CUDA(call)                                    \

@@ -233,10 +233,14 @@ class Graph:
     check(lib.cg_capture_begin(self._h), "cg_capture_begin")
     try:
       body()
-    finally:
+    except BaseException:
+      # end the capture so the stream is usable again; drop what it recorded
       x = ctypes.c_void_p()
-      rc = lib.cg_capture_end(self._h, ctypes.byref(x))
-    check(rc, "cg_capture_end")
+      if lib.cg_capture_end(self._h, ctypes.byref(x)) == 0 and x.value:
+        lib.cg_exec_destroy(x)
+      raise
+    x = ctypes.c_void_p()
+    check(lib.cg_capture_end(self._h, ctypes.byref(x)), "cg_capture_end")
     return Exec(x)
 
   def validate(self, roots, d_levels, d_parents):

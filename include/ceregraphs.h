@@ -80,7 +80,19 @@ typedef struct cg_options {
   int32_t ms_history;       /* multi-source: rounds of frontier history for the output
                                pass (0 = as memory allows, at most 64; < 0 = none: outputs
                                are written during the rounds) */
+  int32_t parent_rule;      /* CG_PARENT_LOWEST (default) or CG_PARENT_FIFO */
 } cg_options;
+
+/* Parent of a vertex at level L+1 (cg_options.parent_rule):
+ *  LOWEST: its lowest-index in-neighbour at level L -- the documented rule of
+ *          the reference's kernel (bfs/README.md:208-224);
+ *  FIFO:   the in-neighbour scipy's breadth_first_order, the reference's host
+ *          check (run_graph500.py:383-395), assigns: the first one dequeued.
+ *          A pass after the search (cg_bfs, cg_bfs_device, cg_msbfs,
+ *          cg_msbfs_device); it synchronises with the handle's stream, so it is
+ *          refused (CG_ERR_NOT_SUPPORTED) while the stream is being captured. */
+#define CG_PARENT_LOWEST 0
+#define CG_PARENT_FIFO 1
 
 #define CG_HISTORY 64
 

@@ -153,3 +153,19 @@ def test_driver_end_to_end(built_lib, tmp_path, mode):
   assert rc == 0
   s = list(csv.DictReader(open(summ)))
   assert len(s) == 2 and s[1]["num_correctness_fail"] == "0" and s[1]["matrix_symmetric"] == "False"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["per-root", "batched"])
+def test_driver_fifo_parents(built_lib, tmp_path, mode):
+  """--parent-rule fifo: scipy's parents, every search still a valid
+  Graph500 tree (the lowest-index rule is not judged)."""
+  import csv
+  from ceregraphs_gb300 import run_graph500
+  out = tmp_path / "rows.csv"
+  rc = run_graph500.main(["--rmat", "12", "16", "0", "--num-searches", "8", "--mode", mode,
+                          "--parent-rule", "fifo", "--csv", str(out), "--quiet"])
+  assert rc == 0
+  rows = list(csv.DictReader(open(out)))
+  assert len(rows) == 8 and all(r["correctness_ok"] == "True" for r in rows)
+  assert all(r["parent_rule"] == "fifo" for r in rows)
