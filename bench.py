@@ -464,8 +464,7 @@ def run_uneven(args):
     k = len(roots)
     tune = autotune.tune(g, a, roots[:128], mode="batched",
                          space={"lane_words": [1, 2], "ms_alpha": [1.0, 4.0, 16.0],
-                                "block_size": [512]}, reps=1, cache=autotune.Cache(
-                                    os.path.join(HERE, "_work", "tune_cache.json")))
+                                "block_size": [512]}, reps=1, cache=autotune.Cache())
     lanes = 64 * g.options().lane_words
     d_lv = torch.empty((k, a.n), dtype=torch.int32, device="cuda")
     d_pa = torch.empty((k, a.n), dtype=torch.int32, device="cuda")
