@@ -916,6 +916,7 @@ __device__ __forceinline__ uint64_t records_mask(const MsParams &p, int64_t v, i
 template <int W>
 __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
   __shared__ int32_t s_list[kScanBlock / 32][kScanWords * 32];
+  __shared__ int32_t s_ru[kScanBlock][kRecords + 1];  // a thread's record sources
   if (*(volatile int *)p.flag || *(volatile int *)&p.ctl->status != 0) return;
   const int rounds = history_rounds(p);
   if (rounds <= 2) return;
@@ -947,14 +948,24 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
       const int np0 = p.pair_n[v];
       int np = np0;
       bool over = false;
+      // the records' sources: a hit from a source already recorded joins its
+      // record (pull rounds record a source again in each round it serves)
+      int32_t *ru = s_ru[threadIdx.x];
+      for (int q = 0; q < np0; ++q) ru[q] = p.pair_u[(int64_t)q * p.n + v];
       for (int h = 0; h < W && 64 * h < p.k; ++h) {
         const uint64_t covered = records_mask<W>(p, v, h, np0);
         scan_in_list<W, kScanG>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
-          if (np < kRecords) {
+          int found = -1;
+          for (int q = 0; q < np && found < 0; ++q)
+            if (ru[q] == u) found = q;
+          if (found >= 0) {
+            p.pair_m[((int64_t)found * p.n + v) * W + h] |= m;
+          } else if (np < kRecords) {
             const int64_t at = (int64_t)np * p.n + v;
             p.pair_u[at] = u;
 #pragma unroll
             for (int w = 0; w < W; ++w) p.pair_m[at * W + w] = w == h ? m : 0ull;
+            ru[np] = u;
             ++np;
           } else {
             over = true;
@@ -970,26 +981,49 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
 }
 
 // Fix-up pass, after the output pass: the lanes of the listed vertices that
-// no record covers get their parents written one by one (a vertex with more
-// distinct parents than kRecords; rare).
+// no record covers (a vertex with more distinct parents than kRecords) get
+// their parents written one by one.  One warp a vertex: lane j holds in-list
+// entry j (a light in-list has at most 32) and gathers that entry's history
+// masks for up to kPre levels at once; the 32 x 64 hit matrix is transposed
+// a 32-lane word at a time (warp_transpose32), so warp lane b finds the first
+// entry -- the lowest-index parent -- of lane b of that word.
 template <int W>
 __global__ void __launch_bounds__(kScanBlock) msbfs_fixup(MsParams p) {
   if (*(volatile int *)p.flag || *(volatile int *)&p.ctl->status != 0) return;
   const unsigned cnt = *(volatile unsigned *)&p.ctl->nover;
   if (cnt == 0) return;
   const int rounds = history_rounds(p);
-  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += nthreads) {
+  const int lane = lane_id();
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp_id_global(); i < cnt; i += nwarps) {
     const int64_t v = p.queue0[i];
     const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
+    const bool has = lane < e - s;
+    const int32_t u = has ? __ldg(p.in_idx + s + lane) : 0;
     const int np = p.pair_n[v];
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
-      const uint64_t covered = records_mask<W>(p, v, h, np);
-      // the whole (<= kPullLight) in-list's loads in flight at once
-      scan_in_list<W, kPullLight>(p, v, h, rounds, s, e, ~covered, [&](int32_t u, uint64_t m) {
-        for (uint64_t x = m; x; x &= x - 1)
-          p.parents[(int64_t)(64 * h + __ffsll((long long)x) - 1) * p.n + v] = u;
-      });
+      uint64_t todo = ~records_mask<W>(p, v, h, np);
+      for (int L0 = 2; L0 < rounds && todo; L0 += kPre) {  // uniform: the whole warp
+        uint64_t pm[kPre];
+#pragma unroll
+        for (int j = 0; j < kPre; ++j)
+          pm[j] = L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] & todo : 0ull;
+        uint64_t hit = 0, batch = 0;
+#pragma unroll
+        for (int j = 0; j < kPre; ++j) {
+          batch |= pm[j];
+          if (pm[j] && has) hit |= pm[j] & plane<W>(p, L0 + j - 1)[(int64_t)u * W + h];
+        }
+        todo &= ~batch;
+        if (!batch) continue;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const uint32_t t = warp_transpose32((uint32_t)(hit >> (32 * half)));
+          const int first = t ? __ffs(t) - 1 : 0;
+          const int32_t par = __shfl_sync(kMsFull, u, first);
+          if (t) p.parents[(int64_t)(64 * h + 32 * half + lane) * p.n + v] = par;
+        }
+      }
     }
   }
 }
@@ -1243,7 +1277,10 @@ int ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d
   const int64_t cap = (int64_t)out_per_sm * g->num_sms;
   if (blocks > cap) blocks = cap;
   msbfs_outputs<W><<<(unsigned)blocks, kOutBlock, smem, g->stream>>>(p);
-  msbfs_fixup<W><<<(unsigned)g->num_sms, kScanBlock, 0, g->stream>>>(p);
+  int fix_per_sm = 0;
+  CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fix_per_sm, msbfs_fixup<W>, kScanBlock, 0));
+  if (fix_per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
+  msbfs_fixup<W><<<(unsigned)(fix_per_sm * g->num_sms), kScanBlock, 0, g->stream>>>(p);
   CG_CUDA(cudaGetLastError());
   return CG_OK;
 }
