@@ -1069,6 +1069,12 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
     const int np = valid && slot < 0 ? p.pair_n[v] : 0;
 #pragma unroll 1
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
+      // the first kPre history planes: independent of the slot and record
+      // loads below, so they are issued first and their latency overlaps
+      uint64_t pm0[kPre];
+#pragma unroll
+      for (int j = 0; j < kPre; ++j)
+        pm0[j] = valid && j < rounds ? plane<W>(p, j)[v * W + h] : 0ull;
       // parents of levels >= 2 of the tile's slotted vertices: the warp copies
       // each slot's 256-byte candidate row into the vertex's tile row, four
       // rows' loads in flight
@@ -1128,15 +1134,14 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
       uint64_t S[kSlices], reached = 0, m01[2] = {0ull, 0ull};
 #pragma unroll
       for (int b = 0; b < kSlices; ++b) S[b] = 0;
+      m01[0] = pm0[0];
+      m01[1] = pm0[1];
       for (int L0 = 0; L0 < rounds; L0 += kPre) {  // uniform: the whole warp
         uint64_t pm[kPre];
 #pragma unroll
         for (int j = 0; j < kPre; ++j)
-          pm[j] = valid && L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] : 0ull;
-        if (L0 == 0) {
-          m01[0] = pm[0];
-          m01[1] = pm[1];
-        }
+          pm[j] = L0 == 0 ? pm0[j]
+                          : (valid && L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] : 0ull);
         // L0 is a multiple of kPre = 8: bits 0..2 of level L0 + j are those
         // of j, known at compile time; bits 3.. those of L0, the same for the
         // whole batch
