@@ -164,3 +164,37 @@ def test_driver_arguments():
   assert a.num_searches == 64 and not a.nocorrectness
   with pytest.raises(SystemExit):
     run_graph500.parse_args(["--num-searches", "3"])   # a graph source is required
+
+
+def test_abi_struct_layouts_match_the_header(tmp_path):
+  """Every ctypes mirror of a struct in include/ceregraphs.h has the C
+  layout: a C program compiled against the header prints each field's offset
+  and each struct's size."""
+  import shutil
+  import subprocess
+  from ceregraphs_gb300 import _lib
+  cc = shutil.which("gcc") or shutil.which("cc")
+  if cc is None:
+    pytest.skip("no C compiler")
+  structs = {"cg_options": _lib.CgOptions, "cg_stats": _lib.CgStats,
+             "cg_edge_list": _lib.CgEdgeList, "cg_validation": _lib.CgValidation}
+  lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "ceregraphs.h"',
+           "int main(void) {"]
+  for cname, cls in structs.items():
+    lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+    for f, _ in cls._fields_:
+      lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+  lines += ["  return 0;", "}"]
+  src = tmp_path / "layout.c"
+  src.write_text("\n".join(lines) + "\n")
+  exe = tmp_path / "layout"
+  inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+  subprocess.check_call([cc, "-std=c99", "-I", inc, str(src), "-o", str(exe)])
+  got = {}
+  for line in subprocess.check_output([str(exe)]).decode().splitlines():
+    name, field, val = line.split()
+    got[(name, field)] = int(val)
+  for cname, cls in structs.items():
+    assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+    for f, _ in cls._fields_:
+      assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
