@@ -665,41 +665,108 @@ __global__ void dead_map_kernel(int64_t n, int64_t words, const int64_t *__restr
   }
 }
 
+int refuse_setup_in_capture(cg_graph *g) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CG_CUDA(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs == cudaStreamCaptureStatusNone) return CG_OK;
+  set_error_text("a handle's first batched search sets up state: run it outside a capture");
+  return CG_ERR_NOT_SUPPORTED;
+}
+
+// A handle's one-time per-root set-up runs on a private stream and is waited
+// for, so it is done once and at once even when the first search is issued
+// inside a capture of the handle's stream (which would only record it).  Work
+// still queued on the handle's stream (the graph upload) is waited for first.
+static int setup_stream(cg_graph *g, cudaStream_t *s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CG_CUDA(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs == cudaStreamCaptureStatusNone) CG_CUDA(cudaStreamSynchronize(g->stream));
+  CG_CUDA(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
+  return CG_OK;
+}
+
+static int setup_wait(cudaStream_t s) {
+  const cudaError_t e = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  return e == cudaSuccess ? CG_OK : cuda_fail(e, "search state set-up");
+}
+
 int dead_prepare(cg_graph *g) {
   if (g->dead) return CG_OK;
   const int64_t words = (g->n + 31) / 32;
-  if (cudaMalloc(&g->dead, sizeof(uint32_t) * (size_t)words) != cudaSuccess) {
-    g->dead = nullptr;
+  uint32_t *dead = nullptr;
+  if (cudaMalloc(&dead, sizeof(uint32_t) * (size_t)words) != cudaSuccess)
     return CG_ERR_OUT_OF_MEMORY;
+  cudaStream_t s = nullptr;
+  int rc = setup_stream(g, &s);
+  if (!rc) {
+    const int64_t blocks = (words + 255) / 256;
+    dead_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(g->n, words,
+                                                                               g->in_off, dead);
+    const cudaError_t e = cudaGetLastError();
+    rc = setup_wait(s);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "dead-vertex map");
   }
+  if (rc) {
+    cudaFree(dead);
+    return rc;
+  }
+  g->dead = dead;
   g->device_bytes += sizeof(uint32_t) * words;
-  const int64_t blocks = (words + 255) / 256;
-  dead_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, g->stream>>>(
-      g->n, words, g->in_off, g->dead);
-  CG_CUDA(cudaGetLastError());
   return CG_OK;
 }
 
 int bfs_prepare(cg_graph *g) {
-  if (g->bitmaps) return CG_OK;
+  if (g->d_stats) return CG_OK;  // the last of the buffers below: all are in place
   int rc = dead_prepare(g);
   if (rc) return rc;
   int dev_coop = 0;
   CG_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, g->device));
   if (!dev_coop) return CG_ERR_NOT_SUPPORTED;
-  g->words = (g->n + 31) / 32;
-  g->bcap = bfs_big_capacity(g->n, g->nnz);
-  const size_t bytes_bm = sizeof(uint32_t) * 4 * (size_t)g->words;
+  const int64_t words = (g->n + 31) / 32;
+  const int64_t bcap = bfs_big_capacity(g->n, g->nnz);
+  const size_t bytes_bm = sizeof(uint32_t) * 4 * (size_t)words;
   const size_t bytes_q = sizeof(int32_t) * 2 * (size_t)g->n;
-  const size_t bytes_b = sizeof(uint32_t) * 2 * (size_t)g->bcap;
-  if (cudaMalloc(&g->bitmaps, bytes_bm) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
-  if (cudaMalloc(&g->queue, bytes_q) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
-  if (cudaMalloc(&g->bigoff, bytes_b) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
-  if (cudaMalloc(&g->ctl, sizeof(BfsCtl)) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
-  if (cudaMalloc(&g->d_stats, sizeof(cg_stats)) != cudaSuccess) return CG_ERR_OUT_OF_MEMORY;
+  const size_t bytes_b = sizeof(uint32_t) * 2 * (size_t)bcap;
+  uint32_t *bitmaps = nullptr, *bigoff = nullptr;
+  int32_t *queue = nullptr;
+  BfsCtl *ctl = nullptr;
+  cg_stats *stats = nullptr;
+  if (cudaMalloc(&bitmaps, bytes_bm) != cudaSuccess || cudaMalloc(&queue, bytes_q) != cudaSuccess ||
+      cudaMalloc(&bigoff, bytes_b) != cudaSuccess || cudaMalloc(&ctl, sizeof(BfsCtl)) != cudaSuccess ||
+      cudaMalloc(&stats, sizeof(cg_stats)) != cudaSuccess) {
+    cudaFree(bitmaps);
+    cudaFree(queue);
+    cudaFree(bigoff);
+    cudaFree(ctl);
+    cudaFree(stats);
+    return CG_ERR_OUT_OF_MEMORY;
+  }
+  cudaStream_t s = nullptr;
+  rc = setup_stream(g, &s);
+  cudaError_t e = cudaSuccess;
+  if (!rc) {
+    e = cudaMemsetAsync(ctl, 0, sizeof(BfsCtl), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(stats, 0, sizeof(cg_stats), s);
+    rc = setup_wait(s);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "search state reset");
+  }
+  if (rc) {
+    cudaFree(bitmaps);
+    cudaFree(queue);
+    cudaFree(bigoff);
+    cudaFree(ctl);
+    cudaFree(stats);
+    return rc;
+  }
+  g->words = words;
+  g->bcap = bcap;
+  g->bitmaps = bitmaps;
+  g->queue = queue;
+  g->bigoff = bigoff;
+  g->ctl = ctl;
+  g->d_stats = stats;
   g->device_bytes += bytes_bm + bytes_q + bytes_b + sizeof(BfsCtl) + sizeof(cg_stats);
-  CG_CUDA(cudaMemsetAsync(g->ctl, 0, sizeof(BfsCtl), g->stream));
-  CG_CUDA(cudaMemsetAsync(g->d_stats, 0, sizeof(cg_stats), g->stream));
   return CG_OK;
 }
 

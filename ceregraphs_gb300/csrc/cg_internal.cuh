@@ -158,6 +158,9 @@ int cuda_fail(cudaError_t e, const char *what);
 void set_error_text(const char *text);
 int bfs_prepare(cg_graph *g);
 int dead_prepare(cg_graph *g);
+// CG_ERR_NOT_SUPPORTED (with a reason) while the handle's stream is being
+// captured: for set-up that has to synchronise the handle's stream.
+int refuse_setup_in_capture(cg_graph *g);
 int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems);
 void msbfs_release(cg_graph *g);
 // Rewrites the parents of a finished search (d_levels final) by the FIFO rule

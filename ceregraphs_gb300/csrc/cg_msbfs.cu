@@ -843,6 +843,8 @@ static int ms_alloc_state(cg_graph *g, int lane_words) {
   if (rc0) return rc0;
   MsState *old = reinterpret_cast<MsState *>(g->ms_ctl);
   if (old && g->ms_lane_words == lane_words && old->hist_opt == g->opt.ms_history) return CG_OK;
+  rc0 = refuse_setup_in_capture(g);
+  if (rc0) return rc0;
   ms_free_state(old);
   g->ms_ctl = nullptr;
   MsState *s = nullptr;
