@@ -982,13 +982,14 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
 
 // Fix-up pass, after the output pass: the lanes of the listed vertices that
 // no record covers (a vertex with more distinct parents than kRecords) get
-// their parents written one by one.  One warp a vertex: lane j holds in-list
-// entry j (a light in-list has at most 32) and gathers that entry's history
-// masks for up to kPre levels at once; the 32 x 64 hit matrix is transposed
-// a 32-lane word at a time (warp_transpose32), so warp lane b finds the first
-// entry -- the lowest-index parent -- of lane b of that word.
+// their parents written one by one.  One warp a vertex, 32 in-list entries
+// at a time in ascending order: lane j holds entry j of the chunk and gathers
+// that entry's history masks for up to kPre levels at once; the 32 x 64 hit
+// matrix is transposed a 32-lane word at a time (warp_transpose32), so warp
+// lane b finds the chunk's first entry -- the lowest-index parent, earlier
+// chunks having had no hit -- of lane b of that word.
 template <int W>
-__global__ void __launch_bounds__(kScanBlock) msbfs_fixup(MsParams p) {
+__global__ void __launch_bounds__(kScanBlock, W == 1 ? 6 : 4) msbfs_fixup(MsParams p) {
   if (*(volatile int *)p.flag || *(volatile int *)&p.ctl->status != 0) return;
   const unsigned cnt = *(volatile unsigned *)&p.ctl->nover;
   if (cnt == 0) return;
@@ -998,30 +999,35 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_fixup(MsParams p) {
   for (int64_t i = warp_id_global(); i < cnt; i += nwarps) {
     const int64_t v = p.queue0[i];
     const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
-    const bool has = lane < e - s;
-    const int32_t u = has ? __ldg(p.in_idx + s + lane) : 0;
     const int np = p.pair_n[v];
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
+      // the lanes no record covers; those reached at a level >= 2 get parents
       uint64_t todo = ~records_mask<W>(p, v, h, np);
-      for (int L0 = 2; L0 < rounds && todo; L0 += kPre) {  // uniform: the whole warp
-        uint64_t pm[kPre];
+      for (int64_t c0 = s; c0 < e && todo; c0 += 32) {  // uniform: the whole warp
+        const bool has = c0 + lane < e;
+        const int32_t u = has ? __ldg(p.in_idx + c0 + lane) : 0;
+        for (int L0 = 2; L0 < rounds && todo; L0 += kPre) {
+          uint64_t pm[kPre];
 #pragma unroll
-        for (int j = 0; j < kPre; ++j)
-          pm[j] = L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] & todo : 0ull;
-        uint64_t hit = 0, batch = 0;
+          for (int j = 0; j < kPre; ++j)
+            pm[j] = L0 + j < rounds ? plane<W>(p, L0 + j)[v * W + h] & todo : 0ull;
+          uint64_t hit = 0, batch = 0;
 #pragma unroll
-        for (int j = 0; j < kPre; ++j) {
-          batch |= pm[j];
-          if (pm[j] && has) hit |= pm[j] & plane<W>(p, L0 + j - 1)[(int64_t)u * W + h];
-        }
-        todo &= ~batch;
-        if (!batch) continue;
+          for (int j = 0; j < kPre; ++j) {
+            batch |= pm[j];
+            if (pm[j] && has) hit |= pm[j] & plane<W>(p, L0 + j - 1)[(int64_t)u * W + h];
+          }
+          if (!batch) continue;
+          uint64_t found = 0;
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          const uint32_t t = warp_transpose32((uint32_t)(hit >> (32 * half)));
-          const int first = t ? __ffs(t) - 1 : 0;
-          const int32_t par = __shfl_sync(kMsFull, u, first);
-          if (t) p.parents[(int64_t)(64 * h + 32 * half + lane) * p.n + v] = par;
+          for (int half = 0; half < 2; ++half) {
+            const uint32_t t = warp_transpose32((uint32_t)(hit >> (32 * half)));
+            const int first = t ? __ffs(t) - 1 : 0;
+            const int32_t par = __shfl_sync(kMsFull, u, first);
+            if (t) p.parents[(int64_t)(64 * h + 32 * half + lane) * p.n + v] = par;
+            found |= (uint64_t)__ballot_sync(kMsFull, t != 0) << (32 * half);
+          }
+          todo &= ~found;
         }
       }
     }
