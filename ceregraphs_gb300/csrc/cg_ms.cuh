@@ -75,6 +75,7 @@ struct MsParams {
   const int32_t *med_vtx;    // [nmed] vertices of in-degree in (kPullLight, kHubDeg]
   int64_t nmed;
   const uint32_t *hub_choff; // [nhub + 1] prefix of in-list chunks
+  const uint32_t *hub_of_chunk; // [chunks] the hub each in-list chunk belongs to
   uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
   uint64_t *hub_found;       // [nhub][W] lanes found this round
   int nhub;
@@ -550,6 +551,7 @@ struct MsState {
   int32_t *med_vtx = nullptr;
   int64_t nmed = 0;
   uint32_t *hub_choff = nullptr;
+  uint32_t *hub_of_chunk = nullptr;
   uint32_t *hub_cand = nullptr;
   uint64_t *hub_found = nullptr;
   MsCtl *ctl = nullptr;
@@ -612,6 +614,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.med_vtx = s->med_vtx;
   p.nmed = s->nmed;
   p.hub_choff = s->hub_choff;
+  p.hub_of_chunk = s->hub_of_chunk;
   p.hub_cand = s->hub_cand;
   p.hub_found = s->hub_found;
   p.nhub = s->nhub;

@@ -185,15 +185,7 @@ __device__ void hub_chunks(const MsParams &p, const uint64_t *cur, const Mask<W>
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const unsigned nchunks = p.hub_choff[p.nhub];
   for (unsigned c = (unsigned)warp_id_global(); c < nchunks; c += (unsigned)nwarps) {
-    unsigned lo = 0, hi = (unsigned)p.nhub - 1;
-    while (lo < hi) {
-      const unsigned mid = (lo + hi + 1) >> 1;
-      if (p.hub_choff[mid] <= c)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const int h = (int)lo;
+    const int h = (int)p.hub_of_chunk[c];
     const int32_t v = p.hub_vtx[h];
     const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v));
     if (!want.any()) continue;
@@ -640,6 +632,7 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->hub_vtx);
   cudaFree(s->med_vtx);
   cudaFree(s->hub_choff);
+  cudaFree(s->hub_of_chunk);
   cudaFree(s->hub_cand);
   cudaFree(s->hub_found);
   cudaFree(s->ctl);
@@ -712,13 +705,31 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
     e = cudaMemcpyAsync(h_chunks + 1, chunks, sizeof(uint32_t) * nhub, cudaMemcpyDeviceToHost,
                         g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    uint32_t *h_owner = nullptr;
+    size_t nchunks = 0;
     if (e == cudaSuccess) {
       for (unsigned h = 0; h < nhub; ++h) h_chunks[h + 1] += h_chunks[h];
-      e = cudaMemcpyAsync(s->hub_choff, h_chunks, sizeof(uint32_t) * (nhub + 1),
-                          cudaMemcpyHostToDevice, g->stream);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+      // chunk -> hub, so a work item finds its hub with one load
+      nchunks = h_chunks[nhub];
+      h_owner = new uint32_t[nchunks ? nchunks : 1];
+      for (unsigned h = 0; h < nhub; ++h)
+        for (uint32_t c = h_chunks[h]; c < h_chunks[h + 1]; ++c) h_owner[c] = h;
+      if (cudaMalloc(&s->hub_of_chunk, sizeof(uint32_t) * (nchunks ? nchunks : 1)) != cudaSuccess)
+        rc = CG_ERR_OUT_OF_MEMORY;
+      if (!rc) e = cudaMemcpyAsync(s->hub_choff, h_chunks, sizeof(uint32_t) * (nhub + 1),
+                                   cudaMemcpyHostToDevice, g->stream);
+      if (!rc && e == cudaSuccess && nchunks)
+        e = cudaMemcpyAsync(s->hub_of_chunk, h_owner, sizeof(uint32_t) * nchunks,
+                            cudaMemcpyHostToDevice, g->stream);
+      if (!rc && e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     }
     delete[] h_chunks;
+    delete[] h_owner;
+    if (rc) {
+      cudaFree(chunks);
+      break;
+    }
+    g->device_bytes += sizeof(uint32_t) * nchunks;
     cudaFree(chunks);
     if (e != cudaSuccess) { rc = cuda_fail(e, "hub chunks"); break; }
     g->device_bytes += sizeof(int32_t) * g->n + sizeof(int32_t) * (cap + mcap) +

@@ -321,15 +321,7 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       const unsigned hi_item = item - nlg - nmg;
       const unsigned c1 = min((hi_item + 1) * kHubGrab, nchunks);
       for (unsigned c = hi_item * kHubGrab; c < c1; ++c) {
-        unsigned lo = 0, hi = (unsigned)p.nhub - 1;
-        while (lo < hi) {
-          const unsigned mid = (lo + hi + 1) >> 1;
-          if (p.hub_choff[mid] <= c)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        const int h = (int)lo;
+        const int h = (int)p.hub_of_chunk[c];
         const int32_t v = p.hub_vtx[h];
         const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
         if (!want.any()) continue;
