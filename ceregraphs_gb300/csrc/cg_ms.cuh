@@ -78,6 +78,10 @@ struct MsParams {
   const uint32_t *hub_of_chunk; // [chunks] the hub each in-list chunk belongs to
   uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
   uint64_t *hub_found;       // [nhub][W] lanes found this round
+  // [nhub] lowest chunk that found every wanted lane, per round (ledger pull):
+  // ((round + 1) << 24) | (0xFFFFFF - chunk), combined with atomicMax; ledger
+  // rounds stay below 255 and chunks below 2^24 (nnz < 2^32, 1024 per chunk)
+  unsigned *hub_done;
   int nhub;
   int32_t *levels, *parents;  // batch mode: lane l at levels + l * n (start round 0)
   const LaneTable *lanes;     // serving pool: per-lane outputs and start rounds
@@ -554,6 +558,7 @@ struct MsState {
   uint32_t *hub_of_chunk = nullptr;
   uint32_t *hub_cand = nullptr;
   uint64_t *hub_found = nullptr;
+  unsigned *hub_done = nullptr;
   MsCtl *ctl = nullptr;
   int *flag = nullptr;        // history overflow flag of the last batch
   int32_t *cand_slot = nullptr;
@@ -617,6 +622,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.hub_of_chunk = s->hub_of_chunk;
   p.hub_cand = s->hub_cand;
   p.hub_found = s->hub_found;
+  p.hub_done = s->hub_done;
   p.nhub = s->nhub;
   p.levels = p.parents = nullptr;
   p.lanes = nullptr;
@@ -648,6 +654,7 @@ inline int ms_reset(const MsState *s, cudaStream_t stream) {
                             stream));
   CG_CUDA(cudaMemsetAsync(s->hub_cand, 0xff, sizeof(uint32_t) * (size_t)nh * 64 * W, stream));
   CG_CUDA(cudaMemsetAsync(s->hub_found, 0, sizeof(uint64_t) * (size_t)nh * W, stream));
+  CG_CUDA(cudaMemsetAsync(s->hub_done, 0, sizeof(unsigned) * (size_t)nh, stream));
   return CG_OK;
 }
 

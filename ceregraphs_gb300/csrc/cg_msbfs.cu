@@ -635,6 +635,7 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->hub_of_chunk);
   cudaFree(s->hub_cand);
   cudaFree(s->hub_found);
+  cudaFree(s->hub_done);
   cudaFree(s->ctl);
   cudaFree(s->flag);
   cudaFree(s->cand_slot);
@@ -689,7 +690,8 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
     const size_t nh = nhub > 0 ? nhub : 1;
     if (cudaMalloc(&s->hub_choff, sizeof(uint32_t) * (nh + 1)) != cudaSuccess ||
         cudaMalloc(&s->hub_cand, sizeof(uint32_t) * nh * 64 * s->lane_words) != cudaSuccess ||
-        cudaMalloc(&s->hub_found, sizeof(uint64_t) * nh * s->lane_words) != cudaSuccess) {
+        cudaMalloc(&s->hub_found, sizeof(uint64_t) * nh * s->lane_words) != cudaSuccess ||
+        cudaMalloc(&s->hub_done, sizeof(unsigned) * nh) != cudaSuccess) {
       rc = CG_ERR_OUT_OF_MEMORY;
       break;
     }
@@ -733,7 +735,7 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
     cudaFree(chunks);
     if (e != cudaSuccess) { rc = cuda_fail(e, "hub chunks"); break; }
     g->device_bytes += sizeof(int32_t) * g->n + sizeof(int32_t) * (cap + mcap) +
-                       nh * (sizeof(uint32_t) * (1 + 64 * s->lane_words + 4) +
+                       nh * (sizeof(uint32_t) * (1 + 64 * s->lane_words + 4 + 1) +
                              sizeof(uint64_t) * s->lane_words);
   } while (0);
   cudaFree(d_count);

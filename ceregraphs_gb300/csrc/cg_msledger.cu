@@ -320,12 +320,16 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     } else {
       const unsigned hi_item = item - nlg - nmg;
       const unsigned c1 = min((hi_item + 1) * kHubGrab, nchunks);
-      // a hub one of this item's chunks found every wanted lane of: its later
-      // chunks hold only higher-index entries, which could not be parents
+      // a hub whose chunk c' < c found every wanted lane: chunk c holds only
+      // higher-index entries, which could not be parents (known to this item
+      // at once, to others through hub_done, tagged with the round)
+      const unsigned tag = (unsigned)(L + 1) << 24;
       int done_h = -1;
       for (unsigned c = hi_item * kHubGrab; c < c1; ++c) {
         const int h = (int)p.hub_of_chunk[c];
         if (h == done_h) continue;
+        const unsigned d = *(volatile unsigned *)(p.hub_done + h);
+        if ((d & 0xFF000000u) == tag && 0xFFFFFFu - (d & 0xFFFFFFu) < c) continue;
         const int32_t v = p.hub_vtx[h];
         const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
         if (!want.any()) continue;
@@ -334,7 +338,10 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         // hub h has candidate slot nmed + h; several warps scan its chunks
         const Mask<W> got = or_warp_first<W>(p, s, e, want, cur,
                                              p.cand + (p.nmed + h) * (64 * W), true);
-        if (got == want) done_h = h;
+        if (got == want) {
+          done_h = h;
+          if (lane == 0) atomicMax(p.hub_done + h, tag | (0xFFFFFFu - c));
+        }
         if (lane == 0) {
 #pragma unroll
           for (int w = 0; w < W; ++w)
