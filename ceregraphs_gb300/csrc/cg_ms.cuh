@@ -76,6 +76,7 @@ struct MsParams {
   int64_t nmed;
   const uint32_t *hub_choff; // [nhub + 1] prefix of in-list chunks
   const uint32_t *hub_of_chunk; // [chunks] the hub each in-list chunk belongs to
+  const uint32_t *hub_chunk_order; // [chunks] chunk ids by rank within their hub, then hub
   uint32_t *hub_cand;        // [nhub][64 W] parent candidates (0xFFFFFFFF = none)
   uint64_t *hub_found;       // [nhub][W] lanes found this round
   // [nhub] lowest chunk that found every wanted lane, per round (ledger pull):
@@ -556,6 +557,7 @@ struct MsState {
   int64_t nmed = 0;
   uint32_t *hub_choff = nullptr;
   uint32_t *hub_of_chunk = nullptr;
+  uint32_t *hub_chunk_order = nullptr;
   uint32_t *hub_cand = nullptr;
   uint64_t *hub_found = nullptr;
   unsigned *hub_done = nullptr;
@@ -620,6 +622,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.nmed = s->nmed;
   p.hub_choff = s->hub_choff;
   p.hub_of_chunk = s->hub_of_chunk;
+  p.hub_chunk_order = s->hub_chunk_order;
   p.hub_cand = s->hub_cand;
   p.hub_found = s->hub_found;
   p.hub_done = s->hub_done;

@@ -34,6 +34,8 @@
 
 #include <new>
 
+#include <vector>
+
 #include "cg_ms.cuh"
 
 namespace cg {
@@ -633,6 +635,7 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->med_vtx);
   cudaFree(s->hub_choff);
   cudaFree(s->hub_of_chunk);
+  cudaFree(s->hub_chunk_order);
   cudaFree(s->hub_cand);
   cudaFree(s->hub_found);
   cudaFree(s->hub_done);
@@ -713,15 +716,31 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
       for (unsigned h = 0; h < nhub; ++h) h_chunks[h + 1] += h_chunks[h];
       // chunk -> hub, so a work item finds its hub with one load
       nchunks = h_chunks[nhub];
-      h_owner = new uint32_t[nchunks ? nchunks : 1];
+      h_owner = new uint32_t[2 * (nchunks ? nchunks : 1)];
+      uint32_t *h_order = h_owner + (nchunks ? nchunks : 1);
       for (unsigned h = 0; h < nhub; ++h)
         for (uint32_t c = h_chunks[h]; c < h_chunks[h + 1]; ++c) h_owner[c] = h;
-      if (cudaMalloc(&s->hub_of_chunk, sizeof(uint32_t) * (nchunks ? nchunks : 1)) != cudaSuccess)
+      // every hub's first chunk, then every hub's second, ...: a pull round's
+      // later chunks mostly start after a hub's earlier ones are done
+      // (counting sort of the chunks by their rank within the hub)
+      uint32_t maxr = 0;
+      for (unsigned h = 0; h < nhub; ++h)
+        maxr = h_chunks[h + 1] - h_chunks[h] > maxr ? h_chunks[h + 1] - h_chunks[h] : maxr;
+      std::vector<uint32_t> at((size_t)maxr + 1, 0u);
+      for (size_t c = 0; c < nchunks; ++c) ++at[c - h_chunks[h_owner[c]] + 1];
+      for (uint32_t r = 1; r <= maxr; ++r) at[r] += at[r - 1];
+      for (size_t c = 0; c < nchunks; ++c) h_order[at[c - h_chunks[h_owner[c]]]++] = (uint32_t)c;
+      if (cudaMalloc(&s->hub_of_chunk, sizeof(uint32_t) * (nchunks ? nchunks : 1)) != cudaSuccess ||
+          cudaMalloc(&s->hub_chunk_order, sizeof(uint32_t) * (nchunks ? nchunks : 1)) !=
+              cudaSuccess)
         rc = CG_ERR_OUT_OF_MEMORY;
       if (!rc) e = cudaMemcpyAsync(s->hub_choff, h_chunks, sizeof(uint32_t) * (nhub + 1),
                                    cudaMemcpyHostToDevice, g->stream);
       if (!rc && e == cudaSuccess && nchunks)
         e = cudaMemcpyAsync(s->hub_of_chunk, h_owner, sizeof(uint32_t) * nchunks,
+                            cudaMemcpyHostToDevice, g->stream);
+      if (!rc && e == cudaSuccess && nchunks)
+        e = cudaMemcpyAsync(s->hub_chunk_order, h_order, sizeof(uint32_t) * nchunks,
                             cudaMemcpyHostToDevice, g->stream);
       if (!rc && e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     }
@@ -731,7 +750,7 @@ static int ms_build_hubs(cg_graph *g, MsState *s) {
       cudaFree(chunks);
       break;
     }
-    g->device_bytes += sizeof(uint32_t) * nchunks;
+    g->device_bytes += 2 * sizeof(uint32_t) * nchunks;
     cudaFree(chunks);
     if (e != cudaSuccess) { rc = cuda_fail(e, "hub chunks"); break; }
     g->device_bytes += sizeof(int32_t) * g->n + sizeof(int32_t) * (cap + mcap) +

@@ -325,7 +325,8 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       // at once, to others through hub_done, tagged with the round)
       const unsigned tag = (unsigned)(L + 1) << 24;
       int done_h = -1;
-      for (unsigned c = hi_item * kHubGrab; c < c1; ++c) {
+      for (unsigned ci = hi_item * kHubGrab; ci < c1; ++ci) {
+        const unsigned c = p.hub_chunk_order[ci];  // by rank within the hub, then hub
         const int h = (int)p.hub_of_chunk[c];
         if (h == done_h) continue;
         const unsigned d = *(volatile unsigned *)(p.hub_done + h);
