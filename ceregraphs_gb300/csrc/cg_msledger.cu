@@ -406,14 +406,25 @@ __device__ __forceinline__ bool lg_relax(const MsParams &p, const Mask<W> &fu, i
   if (!f.any()) return false;
   acc_lanes<W>(acc, f);
   if (slot >= 0) {
+    // lowest source per new lane: read first (a lower one is often there
+    // already), four lanes' reads in flight at a time
     uint32_t *cand = p.cand + (int64_t)slot * (64 * W);
 #pragma unroll
     for (int j = 0; j < W; ++j) {
       uint64_t bits = f.w[j];
       while (bits) {
-        const int b = __ffsll((long long)bits) - 1;
-        bits &= bits - 1;
-        if ((unsigned)u < cand[j * 64 + b]) atomicMin(cand + j * 64 + b, (unsigned)u);
+        int b[4];
+        uint32_t c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          b[k] = bits ? __ffsll((long long)bits) - 1 : -1;
+          bits &= bits ? bits - 1 : 0ull;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = b[k] >= 0 ? cand[j * 64 + b[k]] : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (b[k] >= 0 && (unsigned)u < c[k]) atomicMin(cand + j * 64 + b[k], (unsigned)u);
       }
     }
   }
