@@ -299,14 +299,44 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       }
     } else if (item < nlg + nmg) {
       const unsigned mi = item - nlg;
-      const int64_t j1 = min((int64_t)(mi + 1) * kMedGrab, p.nmed);
-      for (int64_t j = (int64_t)mi * kMedGrab; j < j1; ++j) {
-        const int32_t v = p.med_vtx[j];
-        const Mask<W> want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
-        if (!want.any()) continue;
+      const int64_t j0 = (int64_t)mi * kMedGrab;
+      const int64_t j1 = min(j0 + kMedGrab, p.nmed);
+      // 64 lanes: lanes 0 .. kMedGrab-1 look at the group's vertices at once
+      // (the lanes each still wants and its in-list) and the warp then scans
+      // those wanting any; 128 lanes (more registers): one vertex at a time
+      int32_t vq = 0;
+      Mask<W> wq = Mask<W>::zero();
+      int64_t sq = 0, eq = 0;
+      if (W == 1 && lane < j1 - j0) {
+        vq = p.med_vtx[j0 + lane];
+        wq = active.andnot(ld_mask<W>(p.vis, vq) | ld_mask<W>(cur, vq));
+        sq = __ldg(p.in_off + vq);
+        eq = __ldg(p.in_off + vq + 1);
+      }
+      unsigned pend = W == 1 ? __ballot_sync(kMsFull, wq.any())
+                             : (1u << (unsigned)(j1 - j0)) - 1u;
+      while (pend) {
+        const int t = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const int64_t j = j0 + t;
+        int32_t v;
+        Mask<W> want;
+        int64_t s, e;
+        if (W == 1) {
+          v = __shfl_sync(kMsFull, vq, t);
+#pragma unroll
+          for (int w = 0; w < W; ++w) want.w[w] = __shfl_sync(kMsFull, wq.w[w], t);
+          s = __shfl_sync(kMsFull, sq, t);
+          e = __shfl_sync(kMsFull, eq, t);
+        } else {
+          v = p.med_vtx[j];
+          want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
+          if (!want.any()) continue;
+          s = __ldg(p.in_off + v);
+          e = __ldg(p.in_off + v + 1);
+        }
         // medium vertex j has candidate slot j: its parents of this round go there
-        const Mask<W> got = or_warp_first<W>(p, __ldg(p.in_off + v), __ldg(p.in_off + v + 1),
-                                             want, cur, p.cand + j * (64 * W), false);
+        const Mask<W> got = or_warp_first<W>(p, s, e, want, cur, p.cand + j * (64 * W), false);
         const bool claimed = lane == 0 && got.any();
         int64_t deg = 0;
         if (claimed) {
