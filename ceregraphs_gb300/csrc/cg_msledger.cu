@@ -1,8 +1,10 @@
 // Multi-source BFS with the outputs written after the search ("ledger"
 // mode).  The rounds advance the W-word lane masks -- vis, and the frontier
 // F_L of every round, kept as a history F_0 .. F_D in HBM -- and write no
-// per-(lane, vertex) output.  One output pass after the last round writes
-// every (lane, vertex) output exactly once:
+// per-(lane, vertex) output.  After the last round a scan pass resolves the
+// parents the rounds left open, one output pass writes every (lane, vertex)
+// output exactly once, and a fix-up pass rewrites the few parents that did
+// not fit the per-vertex records:
 //   level(l, v)  = the round L whose F_L[v] holds bit l      (-1 if none)
 //   parent(l, v) = v at level 0, roots[l] at level 1, else the lowest
 //                  in-neighbour u of v with bit l in F_{level - 1}[u]
@@ -19,8 +21,12 @@
 // candidates.  A push round relaxing u -> v takes atomicMin(slot[l], u) for
 // each new lane l (ms_relax); a pull round scans such a vertex's ascending
 // in-list with one warp (or its chunks, for hubs, with several) and records
-// each lane's first hit (or_warp_first).  Vertices of smaller in-degree are
-// resolved in the output pass by their thread's scan of their short in-list.
+// each lane's first hit (or_warp_first).  Vertices of smaller in-degree keep
+// (source, lanes) records: a pull round's thread scan records each entry that
+// brings new lanes (the lowest-index parent of those lanes, the in-list being
+// ascending); the lanes pushes gave them, and those past the pull rounds'
+// records, are resolved by the scan pass (scan_in_list), which appends
+// records; lanes past all records go to the fix-up pass.
 //
 // Rounds: a pull round ORs the frontier masks of a vertex's in-neighbours
 // until every wanted lane is found; a push round ORs frontier masks into
