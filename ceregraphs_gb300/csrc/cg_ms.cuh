@@ -294,47 +294,13 @@ __device__ __forceinline__ Mask<W> first_holder(const Mask<W> &m) {
   return m.andnot(below);
 }
 
-// Edge u -> v of a push round.  Targets get their new lanes ORed into the
-// next mask, and the one thread that first touches v this round queues it.
-// With outputs written during the rounds (Ledger false), hub targets take
+// Edge u -> v of a push round of the direct kernel (outputs written during
+// the rounds).  Targets get their new lanes ORed into the next mask, and the
+// one thread that first touches v this round queues it; hub targets take
 // parent candidates by atomicMin instead.
-template <int W, bool Ledger>
+template <int W>
 __device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, int32_t u,
                                          int32_t v, uint64_t *nxt, uint32_t *touched) {
-  if (Ledger) {
-    // The loads that depend only on v go out together.  A vertex with a
-    // candidate slot takes its parents of this round here: the lowest frontier
-    // source per lane, by atomicMin (after a read, so that hot targets see few
-    // atomics).  The others are found by the output pass's scan of their short
-    // in-lists.
-    const Mask<W> seen = ld_mask<W>(p.vis, v);
-    const Mask<W> have = ld_mask<W>(nxt, v);
-    const int slot = p.cand_slot[v];
-    const uint32_t tw = touched[v >> 5];
-    const Mask<W> f = fu.andnot(seen);
-    if (!f.any()) return false;
-    if (slot >= 0) {
-      uint32_t *cand = p.cand + (int64_t)slot * (64 * W);
-#pragma unroll
-      for (int j = 0; j < W; ++j) {
-        uint64_t bits = f.w[j];
-        while (bits) {
-          const int b = __ffsll((long long)bits) - 1;
-          bits &= bits - 1;
-          if ((unsigned)u < cand[j * 64 + b]) atomicMin(cand + j * 64 + b, (unsigned)u);
-        }
-      }
-    }
-    const Mask<W> add = f.andnot(have);
-#pragma unroll
-    for (int i = 0; i < W; ++i)
-      if (add.w[i])
-        atomicOr(reinterpret_cast<unsigned long long *>(nxt + (int64_t)v * W + i),
-                 (unsigned long long)add.w[i]);
-    const uint32_t tb = 1u << (v & 31);
-    if (tw & tb) return false;
-    return (atomicOr(touched + (v >> 5), tb) & tb) == 0;
-  }
   const Mask<W> f = fu.andnot(ld_mask<W>(p.vis, v));
   if (!f.any()) return false;
   const int h = p.hub_slot[v];
@@ -368,7 +334,7 @@ __device__ __forceinline__ bool ms_relax(const MsParams &p, const Mask<W> &fu, i
   return (atomicOr(touched + (v >> 5), tb) & tb) == 0;
 }
 
-template <int W, bool Ledger>
+template <int W>
 __device__ __forceinline__ void ms_push_step(const MsParams &p, bool valid, const Mask<W> &fu,
                                              int32_t u, int64_t e, uint64_t *nxt,
                                              uint32_t *touched, int32_t *q, uint32_t *boff,
@@ -378,7 +344,7 @@ __device__ __forceinline__ void ms_push_step(const MsParams &p, bool valid, cons
   int64_t deg = 0;
   if (valid) {
     v = __ldg(p.out_idx + e);
-    claimed = ms_relax<W, Ledger>(p, fu, u, v, nxt, touched);
+    claimed = ms_relax<W>(p, fu, u, v, nxt, touched);
     if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
   }
   ms_enqueue(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
@@ -386,7 +352,7 @@ __device__ __forceinline__ void ms_push_step(const MsParams &p, bool valid, cons
 
 // Walks edge positions [x0, x1) of a big-vertex list (vertices q[cap-1-j],
 // prefix offsets boff[j], all of out-degree > 32).
-template <int W, bool Ledger>
+template <int W>
 __device__ void ms_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *nxt,
                               uint32_t *touched, const int32_t *bq, int64_t cap,
                               const uint32_t *boff, unsigned nbig, unsigned x0, unsigned x1,
@@ -428,11 +394,11 @@ __device__ void ms_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *
         fu = ld_mask<W>(cur, vn);
       }
     }
-    ms_push_step<W, Ledger>(p, valid, fu, u, e, nxt, touched, q, qoff, Rn, acc);
+    ms_push_step<W>(p, valid, fu, u, e, nxt, touched, q, qoff, Rn, acc);
   }
 }
 
-template <int W, bool Ledger>
+template <int W>
 __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
                         uint32_t *touched, MsRound *Rc, MsRound *Rn, MsAcc &acc) {
   __shared__ int32_t s_u[kMsBlock / 32][32];
@@ -459,7 +425,7 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   while (item < nitems) {
     if (item < nb) {
       const unsigned x0 = item * chunk;
-      ms_push_chunk<W, Ledger>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0, min(x0 + chunk, big_edges),
+      ms_push_chunk<W>(p, cur, nxt, touched, qc, p.n, bc, nbig, x0, min(x0 + chunk, big_edges),
                        qn, bn, Rn, acc);
     } else {
       const unsigned idx = (item - nb) * 32u + lane;
@@ -500,7 +466,7 @@ __device__ void ms_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
           fu = ld_mask<W>(cur, uu);
           e = s_s[wib][lo] + (t - s_x[wib][lo]);
         }
-        ms_push_step<W, Ledger>(p, valid, fu, uu, e, nxt, touched, qn, bn, Rn, acc);
+        ms_push_step<W>(p, valid, fu, uu, e, nxt, touched, qn, bn, Rn, acc);
       }
       __syncwarp();
     }

@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_persistent(MsParams p) {
         hub_finalize<W>(p, L, nxt, Rn, acc);
       }
     } else {
-      ms_push<W, false>(p, L, cur, nxt, touched, Rc, Rn, acc);
+      ms_push<W>(p, L, cur, nxt, touched, Rc, Rn, acc);
       __syncthreads();
       if (threadIdx.x == 0)
         s_payload = arrive_and_wait(&ctl->wait, &ctl->status, p.timeout_ns, 0u,
