@@ -627,8 +627,9 @@ inline int ms_reset(const MsState *s, cudaStream_t stream) {
   return CG_OK;
 }
 
-// History launch of one batch (cg_msledger.cu): the rounds, then the output
-// pass; sets *s->flag instead if the search outgrows the history.
+// History launch of one batch (cg_msledger.cu): the rounds, then the scan,
+// output and fix-up passes; sets *s->flag instead if the search outgrows the
+// history.
 int ms_ledger_pass(cg_graph *g, MsState *s, const int64_t *roots, int k, int32_t *d_levels,
                    int32_t *d_parents);
 

@@ -974,8 +974,8 @@ int msbfs_launch(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels
     int32_t *lv = d_levels + (int64_t)b * g->n;
     int32_t *pa = d_parents + (int64_t)b * g->n;
     if (s->hist_planes >= 4) {
-      // rounds on masks + one output pass; the direct kernel runs only if the
-      // search outgrew the history
+      // rounds on masks, then the scan, output and fix-up passes; the direct
+      // kernel runs only if the search outgrew the history
       rc = ms_ledger_pass(g, s, roots + b, kk, lv, pa);
       if (!rc) rc = W == 2 ? ms_launch_gated<2>(g, s, roots + b, kk, lv, pa)
                            : ms_launch_gated<1>(g, s, roots + b, kk, lv, pa);
