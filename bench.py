@@ -382,7 +382,8 @@ def run_ours(args):
                "e2e_gteps": float(m.sum() / batch_e2e_s / 1e9), "e2e_ms": batch_e2e_s * 1e3,
                "lanes": 64 * (1 if k <= 64 else 2), "rounds": stb["rounds"],
                "pull_rounds": stb["pull_rounds"], "bit_exact_vs_per_root": same,
-               "launch": "one cooperative kernel per 64/128 roots, replayed as a CUDA graph"}
+               "launch": "per 64/128 roots: the rounds (one cooperative kernel), then the "
+                         "scan, output and fix-up passes, replayed as one CUDA graph"}
     del ref_lv, ref_pa
   clocks = sampler.stop()
 
