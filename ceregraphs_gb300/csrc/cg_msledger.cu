@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
 
 constexpr int kScanBlock = 256;  // scan and fix-up passes: threads a block
 constexpr int kScanWords = 4;    // scan pass: scanmap words a warp takes at a time
-constexpr int kScanG = 4;        // in-list entries loaded together
+constexpr int kScanG = 2;        // in-list entries loaded together (most lanes resolve at the first)
 constexpr int kPre = 8;          // history planes loaded together (the output pass needs 8)
 
 // The planes the rounds filled: F_0 .. F_{rounds - 1} (F_rounds is empty).
