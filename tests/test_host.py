@@ -162,8 +162,13 @@ def test_driver_arguments():
   a = run_graph500.parse_args(["--rmat", "12", "16", "0", "--mode", "batched", "--lanes", "128"])
   assert a.rmat == [12, 16, 0] and a.mode == "batched" and a.lanes == 128
   assert a.num_searches == 64 and not a.nocorrectness
+  assert a.parent_rule == "lowest"
+  assert run_graph500.parse_args(["--rmat", "8", "16", "0", "--parent-rule",
+                                  "fifo"]).parent_rule == "fifo"
   with pytest.raises(SystemExit):
     run_graph500.parse_args(["--num-searches", "3"])   # a graph source is required
+  with pytest.raises(SystemExit):
+    run_graph500.parse_args(["--rmat", "8", "16", "0", "--parent-rule", "last"])
 
 
 def test_abi_struct_layouts_match_the_header(tmp_path):
