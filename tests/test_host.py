@@ -124,6 +124,7 @@ def test_abi_calls_that_need_no_gpu(built_lib):
   assert built_lib.cg_strerror(_lib.CG_ERR_TIMEOUT).decode().startswith("device-side wait")
   opt = _lib.default_options()
   assert opt.direction == _lib.CG_DIR_AUTO and opt.lane_words == 1
+  assert opt.parent_rule == _lib.CG_PARENT_LOWEST
   # argument checks return before any CUDA call
   h = ctypes.c_void_p()
   assert built_lib.cg_graph_create(0, 0, None, None, None, None, 0, ctypes.byref(h)) == \
