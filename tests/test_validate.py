@@ -169,3 +169,23 @@ def test_driver_fifo_parents(built_lib, tmp_path, mode):
   rows = list(csv.DictReader(open(out)))
   assert len(rows) == 8 and all(r["correctness_ok"] == "True" for r in rows)
   assert all(r["parent_rule"] == "fifo" for r in rows)
+
+
+@pytest.mark.gpu
+def test_run_bfs_end_to_end(built_lib, tmp_path, oracle_mod):
+  """The single-search driver on the device: one search, its tree checked,
+  the tie-break count against scipy's rule, a CSV row."""
+  import csv
+  from ceregraphs_gb300 import run_bfs
+  out = tmp_path / "bfs_timing.csv"
+  for extra in ([], ["--directional"], ["--direction", "auto"]):
+    rc = run_bfs.main(["--rmat", "12", "16", "0", "--source", "0", "--csv", str(out)] + extra)
+    assert rc == 0
+  rows = list(csv.DictReader(open(out)))
+  assert len(rows) == 3 and all(r["correctness_ok"] == "True" for r in rows)
+  a = generators.rmat(12, 16, 0)
+  lv, pa, _ = oracle_mod.bfs(*a.out_lists(), a.in_off, a.in_idx, 0)
+  fp = oracle_mod.fifo_parents(a.in_off, a.in_idx, lv, 0)
+  want = int(np.sum((fp != pa) & (lv > 0)))
+  assert all(int(r["scipy_parent_differs"]) == want for r in rows)
+  assert [r["direction"] for r in rows] == ["topdown", "tau", "auto"]
