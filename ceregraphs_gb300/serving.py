@@ -129,12 +129,25 @@ def poisson_arrivals(rate_qps, count, graph_roots, seed=6):
   return out
 
 
+def check_budget(graphs, hbm_budget_bytes):
+  """A budget must admit at least one query of every graph (its levels and
+  parents, 8 bytes a vertex); otherwise that graph's queries would wait
+  forever.  Raises ValueError naming the graph."""
+  if hbm_budget_bytes is None:
+    return
+  for name, g in graphs.items():
+    if 8 * g.n > hbm_budget_bytes:
+      raise ValueError(f"HBM budget of {hbm_budget_bytes} bytes is below one query's "
+                       f"outputs on graph {name!r} ({8 * g.n} bytes)")
+
+
 class Server:
   """Continuous batching over one pool per resident graph."""
 
   def __init__(self, graphs, lane_words=1, hbm_budget_bytes=None, max_rounds=0,
                on_done=None):
     import torch
+    check_budget(graphs, hbm_budget_bytes)
     self.torch = torch
     self.graphs = graphs                      # name -> engine.Graph
     self.lane_words = lane_words
@@ -233,6 +246,7 @@ class BatchServer:
 
   def __init__(self, graphs, lane_words=1, hbm_budget_bytes=None, batch_min=4, on_done=None):
     import torch
+    check_budget(graphs, hbm_budget_bytes)
     self.torch = torch
     self.graphs = graphs
     self.lanes = 64 * int(lane_words)

@@ -185,3 +185,19 @@ def test_batch_server_equals_alone(built_lib, batch_min):
   assert s["p99_ms"] >= s["p50_ms"] > 0
   for g in graphs.values():
     g.close()
+
+
+def test_budget_below_one_query_is_refused():
+  """A graph whose single query does not fit the HBM budget would never be
+  served: both servers refuse such a budget up front."""
+  import types
+  from ceregraphs_gb300 import serving
+  graphs = {"small": types.SimpleNamespace(n=1000), "big": types.SimpleNamespace(n=10 ** 6)}
+  serving.check_budget(graphs, None)
+  serving.check_budget(graphs, 8 * 10 ** 6)
+  with pytest.raises(ValueError, match="big"):
+    serving.check_budget(graphs, 8 * 10 ** 6 - 1)
+  with pytest.raises(ValueError):
+    serving.BatchServer(graphs, hbm_budget_bytes=100)
+  with pytest.raises(ValueError):
+    serving.Server(graphs, hbm_budget_bytes=100)
