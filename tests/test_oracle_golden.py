@@ -154,3 +154,31 @@ def test_oracle_fifo_parents_match_scipy(oracle_mod):
     fp = oracle_mod.fifo_parents(D.indptr, D.indices, ARR[f"dir600_r{r}_levels"], r)
     assert np.array_equal(fp, ARR[f"dir600_r{r}_scipy_parents"])
     assert oracle_mod.graph500_validate(D, r, ARR[f"dir600_r{r}_levels"], fp) == []
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_against_scipy_on_random_graphs(oracle_mod, seed):
+  """Seeded random graphs (directed and symmetric, with self-loops, isolated
+  vertices and several components): the C restatement's levels, the
+  lowest-index parents and the FIFO restatement all equal what scipy's
+  breadth_first_order (the reference's host search) gives."""
+  rng = np.random.default_rng(1000 + seed)
+  n = int(rng.integers(20, 400))
+  e = int(rng.integers(n // 2, 4 * n))
+  src = rng.integers(0, n, e)
+  dst = rng.integers(0, n, e)
+  if seed % 2:
+    src, dst = np.concatenate([src, dst]), np.concatenate([dst, src])
+  A = sparse.coo_matrix((np.ones(len(src)), (dst, src)), shape=(n, n)).tocsr()
+  A.sum_duplicates()
+  A.data[:] = 1.0
+  A.sort_indices()
+  for r in rng.choice(n, size=4, replace=False):
+    r = int(r)
+    lv, pa, rounds = oracle_mod.bfs_csr(A, r)
+    sl, sp, _ = oracle_mod.scipy_bfs(A, r)
+    assert np.array_equal(lv, sl)
+    assert np.array_equal(pa, oracle_mod.min_parents(A, sl, r))
+    assert np.array_equal(oracle_mod.fifo_parents(A.indptr, A.indices, sl, r),
+                          sp.astype(np.int32))
+    assert oracle_mod.graph500_validate(A, r, lv, pa) == []
