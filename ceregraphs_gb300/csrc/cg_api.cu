@@ -79,7 +79,7 @@ using namespace cg;
 
 extern "C" {
 
-int cg_version(void) { return 10000; }
+int cg_version(void) { return 10100; }
 
 const char *cg_strerror(int status) {
   switch (status) {

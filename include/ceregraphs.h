@@ -113,6 +113,8 @@ typedef struct cg_stats {
 } cg_stats;
 
 /* ---- library ---------------------------------------------------------- */
+/* 10000 * major + 100 * minor: 1.1 (10100) added cg_options.parent_rule at the
+ * end of cg_options -- a caller with the 1.0 struct must allocate the new size. */
 int cg_version(void);
 const char *cg_strerror(int status);
 /* Text of the last error seen by this thread: a CUDA error, or why a size was
