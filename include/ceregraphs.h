@@ -181,7 +181,10 @@ int cg_count_edges(cg_graph *g, const int32_t *d_levels, int32_t k, int64_t *m_o
  * Capture the searches enqueued on a handle's stream (cg_bfs_device,
  * cg_msbfs_device) between begin and end into one executable CUDA graph, and
  * replay it with one launch.  The captured searches keep the roots and
- * output pointers they were given. */
+ * output pointers they were given.  Refused with CG_ERR_NOT_SUPPORTED while
+ * capturing: a handle's first batched search at a lane width (its state is
+ * set up with stream synchronisations; run one outside the capture first) and
+ * searches under CG_PARENT_FIFO. */
 typedef struct cg_exec cg_exec;
 int cg_capture_begin(cg_graph *g);
 int cg_capture_end(cg_graph *g, cg_exec **out);
