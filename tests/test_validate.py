@@ -131,6 +131,30 @@ def test_device_validator_at_scale(built_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("lane_words", [1, 2])
+def test_batched_trees_at_the_benchmark_scale(built_lib, lane_words):
+  """The benchmark's graph (R-MAT s21 ef16 seed 0, drawn on the device) and
+  its 64 Graph500 roots (seed 1), plus 64 more for 128 lanes: every batched
+  search passes the Graph500 checks and the lowest-index rule on the device,
+  a size-independent property where the oracle would take minutes."""
+  import torch
+  from ceregraphs_gb300 import graph500
+  g, _ = generators.rmat_device(21, 16, 0, export=False)
+  a = g.export()
+  k = 64 * lane_words
+  roots = graph500.pick_sources(a, k, 1)
+  g.set_options(lane_words=lane_words)
+  lv = torch.empty((k, a.n), dtype=torch.int32, device="cuda")
+  pa = torch.empty_like(lv)
+  torch.cuda.synchronize()
+  g.msbfs_device(roots, lv, pa)
+  assert g.last_stats()["status"] == 0
+  res = g.validate(roots, lv, pa)
+  assert all(r[c]["failures"] == 0 for r in res for c in CHECKS)
+  g.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["per-root", "batched"])
 def test_driver_end_to_end(built_lib, tmp_path, mode):
   """The run_graph500 driver: R-MAT and a graph file, every search checked on
