@@ -1,18 +1,21 @@
 """Graph500-style BFS benchmark on one GB300 (or N replicas).
 
-Workload (default): RMAT scale 21, edgefactor 16, A/B/C/D = .57/.19/.19/.05,
-seed 0, symmetrised and deduplicated; 64 roots drawn with the Graph500 rule
-(seed 1); one direction-optimizing search per root.  A step = the 64
-searches.  Metric: harmonic-mean GTEPS over the roots, m counted with the
-reference's undirected-dedup rule (bfs_timing.py:379-398).
+Workload (default): RMAT scale 23, edgefactor 16, A/B/C/D = .57/.19/.19/.05,
+seed 2, symmetrised and deduplicated (the reference generator's recipe, drawn
+on the GPU bit for bit); 64 roots drawn with the Graph500 rule (seed 3).  A
+step = one direction-optimizing search per root.  Metric: harmonic-mean GTEPS
+over the roots, m counted with the reference's undirected-dedup rule
+(bfs_timing.py:379-398), identical in both arms.
 
 * value: each search timed with CUDA events on the handle's stream, outputs
   (levels + parents) left in HBM.
 * e2e: the same searches through the C ABI call cg_bfs with page-locked host
-  buffers: launch + every round + parent array copied to host memory (the
-  Graph500 Kernel-2 rule), timed on the host clock.
+  buffers: launch + every round + parent array in host memory (the Graph500
+  Kernel-2 rule, run_graph500.py:325-358), timed on the host clock.
+* batched: the same roots as 64 bit lanes of one batched search replayed as a
+  CUDA graph, compared with the per-root loop (GTEPS = sum of m / batch time).
 * --impl reference: the reference's own host BFS (scipy breadth_first_order
-  on A^T, run_graph500.py:383-395), one search per host core in parallel.
+  on A^T, run_graph500.py:383-395), one search at a time on one core.
 
 Prints one JSON line (rank 0).
 """
@@ -31,9 +34,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-# DRAM bytes (read + write) per launch of bfs_persistent, the mean over the 64
-# searches of the default workload measured with ncu (profiles/
-# bfs_persistent_rmat21.md); reported as roofline.traffic for that workload.
+METRIC = "per-root BFS GTEPS, harmonic mean over the Graph500 roots"
+
+# DRAM bytes (read + write) per launch of bfs_persistent measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, mean over the timed step's
+# launches) for (scale, edgefactor, seed, root seed); roofline.traffic.
 NCU_TRAFFIC_BYTES = {(21, 16, 0, 1): 76.9e6}
 FALLBACK_HBM_GBS = 6800.0
 
@@ -44,11 +49,11 @@ def parse():
   ap.add_argument("--steps", type=int, default=5)
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-  ap.add_argument("--scale", type=int, default=21)
+  ap.add_argument("--scale", type=int, default=23)
   ap.add_argument("--edgefactor", type=int, default=16)
-  ap.add_argument("--seed", type=int, default=0)
+  ap.add_argument("--seed", type=int, default=2)
   ap.add_argument("--roots", type=int, default=64)
-  ap.add_argument("--root-seed", type=int, default=1)
+  ap.add_argument("--root-seed", type=int, default=3)
   ap.add_argument("--direction", default="auto", choices=["auto", "topdown", "bottomup", "tau"])
   ap.add_argument("--cpu-seconds", type=float, default=15.0,
                   help="bound on the CPU-baseline sample")
@@ -63,7 +68,7 @@ def parse():
   ap.add_argument("--serving-scales", default="20,22,24,26")
   ap.add_argument("--serving-rates", default="100,1000,10000,100000")
   ap.add_argument("--serving-seconds", type=float, default=2.0,
-                  help="arrival window per rate (query count capped at 4000)")
+                  help="arrival window per rate")
   return ap.parse_args()
 
 
@@ -82,6 +87,15 @@ def peaks():
     return float(d["hbm_gbs"]), "measured"
   except Exception:
     return FALLBACK_HBM_GBS, "fallback"
+
+
+def roofline(achieved_gbs, traffic, kernel, formula):
+  peak, kind = peaks()
+  return {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
+          "frac": achieved_gbs / peak, "traffic": traffic, "kernel": kernel,
+          "peak_source": ("of measured (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured"
+                          else "of fallback 6.8 TB/s"),
+          "algorithmic_bytes": formula}
 
 
 class ClockSampler:
@@ -103,6 +117,7 @@ class ClockSampler:
           stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
     except Exception:
       self.proc = None
+    return self
 
   def stop(self):
     if self.proc is None:
@@ -113,6 +128,7 @@ class ClockSampler:
     except Exception:
       self.proc.kill()
       out, _ = self.proc.communicate()
+    self.proc = None
     sm, smax, reasons = [], 0.0, set()
     names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
     for line in out.strip().splitlines():
@@ -152,17 +168,14 @@ def make_graph_device(args):
   return g, a, time.perf_counter() - t0
 
 
-def workload_config(args, a, extra=None):
-  cfg = {"workload": f"rmat{args.scale}-e{args.edgefactor}-seed{args.seed}, "
-                     f"{args.roots} Graph500 roots (seed {args.root_seed}), one "
-                     f"{args.direction} search per root",
-         "scale": args.scale, "edgefactor": args.edgefactor, "n": a.n, "nnz": a.nnz,
-         "roots": args.roots, "root_seed": args.root_seed, "direction": args.direction,
-         "l2": f"inputs larger than L2: CSR {(a.nnz * 4 + (a.n + 1) * 8) / 1e6:.0f} MB",
-         "parallelism": f"replicas{args.gpus}"}
-  if extra:
-    cfg.update(extra)
-  return cfg
+def workload_config(args, n, nnz):
+  """The workload, identical in both arms."""
+  return {"workload": f"rmat{args.scale}-e{args.edgefactor}-seed{args.seed}, {args.roots} "
+                      f"Graph500 roots (seed {args.root_seed}), one search per root",
+          "scale": args.scale, "edgefactor": args.edgefactor, "n": int(n), "nnz": int(nnz),
+          "roots": args.roots, "root_seed": args.root_seed,
+          "l2": f"inputs larger than L2: CSR {(nnz * 4 + (n + 1) * 8) / 1e6:.0f} MB",
+          "parallelism": f"replicas{args.gpus}"}
 
 
 # --------------------------------------------------------------------------
@@ -171,10 +184,12 @@ def workload_config(args, a, extra=None):
 _REF = {}
 
 
-def _ref_init(indptr, indices, n):
+def _ref_init(a):
+  """A^T in CSR, built once outside any timing (the reference rebuilds it per
+  search, run_graph500.py:384).  For a symmetric A it is A's own CSR."""
   from scipy import sparse
-  A = sparse.csr_matrix((np.ones(len(indices), dtype=np.int8), indices, indptr), shape=(n, n))
-  _REF["At"] = A.transpose().tocsr()
+  A = sparse.csr_matrix((np.ones(a.nnz, dtype=np.int8), a.in_idx, a.in_off), shape=(a.n, a.n))
+  _REF["At"] = A if a.symmetric else A.transpose().tocsr()
 
 
 def _ref_search(root):
@@ -187,70 +202,75 @@ def _ref_search(root):
   return int(root), dt, visited
 
 
-def cpu_reference_sample(a, roots, seconds_budget, processes):
-  """Runs scipy BFS over roots (one per worker), stopping when the budget is
-  spent; returns per-root (root, seconds, m)."""
-  import multiprocessing as mp
+def cpu_reference_sample(a, roots, seconds_budget):
+  """scipy BFS over roots one at a time (one core), stopping once the budget is
+  spent; returns per-search (root, seconds, m)."""
   from ceregraphs_gb300.graph500 import EdgeCounter
   counter = EdgeCounter(a)
-  _ref_init(a.in_off, a.in_idx, a.n)
+  _ref_init(a)
   out = []
   t_start = time.perf_counter()
-  if processes <= 1:
-    for r in roots:
-      root, dt, visited = _ref_search(r)
-      out.append((root, dt, counter.m(visited)))
-      if time.perf_counter() - t_start > seconds_budget:
-        break
-    return out, 1
+  for r in roots:
+    root, dt, visited = _ref_search(r)
+    out.append((root, dt, counter.m(visited)))
+    if time.perf_counter() - t_start > seconds_budget:
+      break
+  return out
+
+
+def cpu_reference_all_cores(roots, processes):
+  """One round of `processes` concurrent scipy searches (one per core, forked
+  after _ref_init); returns (searches, wall seconds, per-search seconds)."""
+  import multiprocessing as mp
   ctx = mp.get_context("fork")
+  t0 = time.perf_counter()
   with ctx.Pool(processes) as pool:
-    i = 0
-    while i < len(roots):
-      batch = roots[i:i + processes]
-      for root, dt, visited in pool.map(_ref_search, batch):
-        out.append((root, dt, counter.m(visited)))
-      i += len(batch)
-      if time.perf_counter() - t_start > seconds_budget:
-        break
-  return out, processes
+    res = pool.map(_ref_search, roots[:processes])
+  return res, time.perf_counter() - t0
 
 
 def run_reference(args):
-  rank, world, _ = dist_env()
+  """The reference's CPU path on this machine: scipy breadth_first_order on A^T,
+  one search per step, one core (the search is single-threaded C)."""
+  rank, _, _ = dist_env()
   if rank != 0:
     return 0
   from ceregraphs_gb300.bfs_timing import harmonic_mean
-  from ceregraphs_gb300.graph500 import pick_sources
-  a, _ = make_graph(args)
+  from ceregraphs_gb300.graph500 import EdgeCounter, pick_sources
+  a, gen_s = make_graph(args)
   roots = pick_sources(a, args.roots, args.root_seed)
-  cores = os.cpu_count() or 1
-  # warmup: one search per worker (bounded)
-  per_step = max(1, min(len(roots), cores))
-  cpu_reference_sample(a, roots[:per_step], 1e9, min(cores, per_step))
-  t0 = time.perf_counter()
+  counter = EdgeCounter(a)
+  _ref_init(a)
+  for s in range(args.warmup):
+    _ref_search(roots[s % len(roots)])
   samples = []
+  t0 = time.perf_counter()
   for s in range(args.steps):
-    sel = [roots[(s * per_step + j) % len(roots)] for j in range(per_step)]
-    res, used = cpu_reference_sample(a, sel, 1e9, min(cores, per_step))
-    samples.extend(res)
+    root, dt, visited = _ref_search(roots[s % len(roots)])
+    samples.append((root, dt, counter.m(visited)))
   wall = time.perf_counter() - t0
-  g = [m / dt / 1e9 for (_, dt, m) in samples]
-  value = harmonic_mean(g)
-  line = {"metric": "GTEPS (harmonic mean over roots), per-root search",
-          "value": value, "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps,
-          "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+  value = harmonic_mean([m / dt / 1e9 for (_, dt, m) in samples])
+  cores = os.cpu_count() or 1
+  # all host cores at once (contended memory): aggregate throughput only
+  par, par_wall = cpu_reference_all_cores(roots, min(cores, len(roots)))
+  par_m = sum(counter.m(v) for (_, _, v) in par)
+  line = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": args.gpus,
+          "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-          "data": "synthetic (RMAT, reference generator recipe)", "impl": "reference",
-          "config": workload_config(args, a, {"parallelism": "host cores"}),
-          "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": min(cores, per_step),
-                           "kind": "reference",
-                           "sample": f"{len(samples)} searches ({per_step} per step, one per "
-                                     "core) of scipy.sparse.csgraph.breadth_first_order on A^T, "
-                                     "the call of run_graph500.py:383-395"},
+          "data": "synthetic (R-MAT, the reference generator's recipe, bit-identical)",
+          "impl": "reference", "config": workload_config(args, a.n, a.nnz),
+          "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": 1, "kind": "reference",
+                           "sample": f"{len(samples)} searches, one per step, one at a time: "
+                                     "scipy.sparse.csgraph.breadth_first_order on A^T, the call "
+                                     "of run_graph500.py:383-395 (single-threaded C); roots "
+                                     "in Graph500 order, cycled"},
           "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0,
                   "d2h_bytes_per_step": 0},
-          "aggregate_gteps_all_cores": sum(m for (_, _, m) in samples) / wall / 1e9}
+          "construction_s": round(gen_s, 2),
+          "all_cores": {"processes": len(par), "host_cores": cores,
+                        "aggregate_gteps": par_m / par_wall / 1e9,
+                        "per_search_hm_gteps_contended": harmonic_mean(
+                            [counter.m(v) / dt / 1e9 for (_, dt, v) in par])}}
   print(json.dumps(line), flush=True)
   return 0
 
@@ -267,14 +287,15 @@ def run_ours(args):
     import torch.distributed as dist
     dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-  from ceregraphs_gb300 import _lib
+  from ceregraphs_gb300 import _lib, replicas
   from ceregraphs_gb300.bfs_timing import harmonic_mean
-  from ceregraphs_gb300.engine import Graph, PinnedBuffer
+  from ceregraphs_gb300.engine import PinnedBuffer
   from ceregraphs_gb300.graph500 import EdgeCounter, pick_sources
 
   g, a, gen_s = make_graph_device(args)
   roots_all = pick_sources(a, args.roots, args.root_seed)
-  roots = roots_all  # every replica runs the full root set (weak scaling)
+  # replicas: each GPU holds the whole graph and takes a disjoint share of roots
+  roots = replicas.shard(roots_all, rank, world)
   dirmap = {"auto": _lib.CG_DIR_AUTO, "topdown": _lib.CG_DIR_TOPDOWN,
             "bottomup": _lib.CG_DIR_BOTTOMUP, "tau": _lib.CG_DIR_TAU}
   g.set_options(direction=dirmap[args.direction])
@@ -301,6 +322,7 @@ def run_ours(args):
   deg_t = torch.from_numpy(np.diff(a.out_lists()[0])).cuda()
   nnz_vis = np.array([int(((d_lv[i] >= 0).to(torch.int64) * deg_t).sum()) for i in range(k)])
   alg_bytes = 4 * nnz_vis + 8 * (n + 1) + 8 * n   # B_1 per search
+  del deg_t
 
   def one_step(ev):
     for i, r in enumerate(roots):
@@ -314,8 +336,7 @@ def run_ours(args):
     one_step(events)
   torch.cuda.synchronize()
 
-  sampler = ClockSampler(local)
-  sampler.start()
+  sampler = ClockSampler(local).start()
   time.sleep(0.3)
   if dist is not None:
     dist.barrier()
@@ -338,21 +359,25 @@ def run_ours(args):
   # e2e: C ABI with host (page-locked) parent buffers, host clock per search
   pin = PinnedBuffer(n)
   e2e_s = np.zeros(k)
-  for i, r in enumerate(roots[:4]):  # warm
+  for r in roots[:4]:  # warm
     g.bfs(r, None, pin.array, want_levels=False)
   for _ in range(args.steps):
     for i, r in enumerate(roots):
       t0 = time.perf_counter()
       _, _, st2 = g.bfs(r, None, pin.array, want_levels=False)
       e2e_s[i] += time.perf_counter() - t0
+      if st2["status"] != 0:
+        raise RuntimeError(f"search failed: {st2}")
   e2e_s /= args.steps
+  pin.free()
 
   # batched: the same roots as bit lanes (64 or 128 per pass), one CUDA graph
   # per step; every lane is checked against the per-root outputs
   batched = None
   if not args.no_batched:
     ref_lv, ref_pa = d_lv.clone(), d_pa.clone()
-    g.set_options(lane_words=1 if k <= 64 else 2)
+    lane_words = 1 if k <= 64 else 2
+    g.set_options(lane_words=lane_words)
     g.msbfs_device(roots, d_lv, d_pa)
     g.last_stats()
     exe = g.capture(lambda: g.msbfs_device(roots, d_lv, d_pa))
@@ -369,70 +394,82 @@ def run_ours(args):
     stb = g.last_stats()
     same = bool(torch.equal(ref_lv, d_lv) and torch.equal(ref_pa, d_pa))
     exe.close()
+    del ref_lv, ref_pa
     pin_lv, pin_pa = PinnedBuffer((k, n)), PinnedBuffer((k, n))
     g.msbfs(roots, pin_lv.array, pin_pa.array)
     t0 = time.perf_counter()
     for _ in range(args.steps):
       g.msbfs(roots, pin_lv.array, pin_pa.array)
     batch_e2e_s = (time.perf_counter() - t0) / args.steps
+    pin_lv.free()
+    pin_pa.free()
     batched_gteps = float(m.sum() / (batch_ms * 1e-3) / 1e9)
     hm_per_root = harmonic_mean(m / (per_root_ms * 1e-3) / 1e9)
+    lanes = 64 * lane_words
+    bk = 4 * a.nnz + 8 * (n + 1) + stb["rounds"] * 2 * n * lanes // 8 + 8 * n * k
     batched = {"gteps": batched_gteps, "ms": batch_ms,
                "vs_per_root_harmonic_mean": batched_gteps / hm_per_root,
                "e2e_gteps": float(m.sum() / batch_e2e_s / 1e9), "e2e_ms": batch_e2e_s * 1e3,
-               "lanes": 64 * (1 if k <= 64 else 2), "rounds": stb["rounds"],
+               "e2e_d2h_bytes": 2 * 4 * n * k,
+               "lanes": lanes, "rounds": stb["rounds"],
                "pull_rounds": stb["pull_rounds"], "bit_exact_vs_per_root": same,
+               "roofline": roofline(bk / (batch_ms * 1e-3) / 1e9, None,
+                                    "msbfs_ledger + msbfs_scan + msbfs_outputs + msbfs_fixup",
+                                    "B_k = 4*nnz + 8*(n+1) + rounds*2*n*lanes/8 + 8*n*k per "
+                                    "batch"),
                "launch": "per 64/128 roots: the rounds (one cooperative kernel), then the "
                          "scan, output and fix-up passes, replayed as one CUDA graph"}
-    del ref_lv, ref_pa
   clocks = sampler.stop()
 
   gteps_dev = m / (per_root_ms * 1e-3) / 1e9
   gteps_e2e = m / e2e_s / 1e9
+  step_ms = wall / args.steps * 1e3
+  m_step = float(m.sum())
+  if dist is not None:
+    from ceregraphs_gb300.replicas import gather
+    gteps_dev = np.array(gather(list(gteps_dev)))
+    gteps_e2e = np.array(gather(list(gteps_e2e)))
+    t = torch.tensor([step_ms, m_step], device="cuda", dtype=torch.float64)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    step_ms, m_step = float(tmax[0].item()), float(t[1].item())
   value = harmonic_mean(gteps_dev)
   e2e_value = harmonic_mean(gteps_e2e)
-  step_ms = wall / args.steps * 1e3
-  if dist is not None:
-    t = torch.tensor([step_ms], device="cuda", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    step_ms = float(t.item())
-  peak, peak_kind = peaks()
   achieved = float(alg_bytes.sum() / (per_root_ms.sum() * 1e-3) / 1e9)
   traffic = NCU_TRAFFIC_BYTES.get((args.scale, args.edgefactor, args.seed, args.root_seed))
   line = {
-      "metric": "GTEPS (harmonic mean over 64 roots), per-root direction-optimizing search",
-      "value": value * world, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+      "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
       "warmup": max(args.warmup, 3), "ms_per_step": step_ms, "higher_is_better": True,
       "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-      "data": "synthetic (RMAT, the reference generator's recipe, bit-identical)",
-      "config": workload_config(args, a, {"generation_and_construction_s": round(gen_s, 3)}),
-      "e2e": {"value": e2e_value * world, "unit": "GTEPS", "h2d_bytes_per_step": 8 * k,
+      "data": "synthetic (R-MAT, the reference generator's recipe, bit-identical)",
+      "config": workload_config(args, n, a.nnz),
+      "construction_s": round(gen_s, 3),
+      "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": 8 * k,
               "d2h_bytes_per_step": 4 * n * k,
-              "note": "cg_bfs: launch + all rounds + parents copied to page-locked host memory"},
+              "note": "cg_bfs: launch + all rounds + parents in page-locked host memory"},
       "gpu_launches": k * args.steps,
-      "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                   "frac": achieved / peak, "traffic": traffic,
-                   "kernel": "bfs_persistent",
-                   "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
-                   "measured" else "fallback 6.8 TB/s",
-                   "algorithmic_bytes": "4*nnz_visited + 8*(n+1) + 8*n per search"},
-      "per_root": {"ms_median": float(np.median(per_root_ms)),
+      "roofline": roofline(achieved, traffic, "bfs_persistent",
+                           "4*nnz_visited + 8*(n+1) + 8*n per search"),
+      "per_root": {"direction": args.direction, "ms_median": float(np.median(per_root_ms)),
                    "ms_min": float(per_root_ms.min()), "ms_max": float(per_root_ms.max()),
                    "gteps_min": float(gteps_dev.min()), "gteps_max": float(gteps_dev.max()),
                    "e2e_ms_median": float(np.median(e2e_s) * 1e3),
                    "rounds": st["rounds"], "pull_rounds_last": st["pull_rounds"]},
+      "aggregate_gteps": m_step / (step_ms * 1e-3) / 1e9,
   }
   if batched:
     line["batched"] = batched
   if clocks:
     line["clocks"] = clocks
   if rank == 0 and not args.no_cpu_baseline:
-    res, used = cpu_reference_sample(a, roots, args.cpu_seconds, 1)
+    res = cpu_reference_sample(a, roots, args.cpu_seconds)
     g_cpu = [mm / dt / 1e9 for (_, dt, mm) in res]
     line["cpu_baseline"] = {
         "value": harmonic_mean(g_cpu), "unit": "GTEPS", "cores": 1, "kind": "reference",
-        "sample": f"{len(res)} of the {k} roots, scipy breadth_first_order on A^T "
-                  f"(run_graph500.py:383-395), single-threaded, {os.cpu_count()} host cores seen"}
+        "sample": f"{len(res)} of the {k} roots, one at a time: scipy breadth_first_order on "
+                  f"A^T (run_graph500.py:383-395), single-threaded, {os.cpu_count()} host "
+                  "cores seen"}
   g.close()
   if rank == 0:
     print(json.dumps(line), flush=True)

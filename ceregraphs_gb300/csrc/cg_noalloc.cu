@@ -44,17 +44,21 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 static std::mutex g_setup_mu;
-static void *g_scratch_addr[kMaxDevices] = {};
 static int g_grid[kMaxDevices] = {};
 
-// Once per device, with that device current: the device address of the
-// scratch array (host code cannot use the symbol itself) and the grid size.
+// With the device current: the device address of the scratch array (host code
+// cannot use the symbol itself, whose host-side name is only a stand-in) and
+// the grid size.  The address is looked up on every call -- the lookup is a
+// host-side table read -- so a cudaDeviceReset between calls, which reloads
+// the module and may move the array, leaves no stale address behind.  The
+// grid size (SM count times resident blocks per SM) is fixed per device and
+// computed once.
 static int noalloc_setup(int dev, void **scratch, int *grid) {
+  void *addr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
   std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
-    void *addr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  if (!g_grid[dev]) {
     int sms = 0, per_sm = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
@@ -62,11 +66,21 @@ static int noalloc_setup(int dev, void **scratch, int *grid) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (per_sm <= 0) return CG_ERR_NOT_SUPPORTED;
     g_grid[dev] = per_sm * sms;
-    g_scratch_addr[dev] = addr;
   }
-  *scratch = g_scratch_addr[dev];
+  *scratch = addr;
   *grid = g_grid[dev];
   return CG_OK;
+}
+
+// True when `p` is page-locked host memory the GPU can write (cudaHostAlloc,
+// cudaHostRegister, cg_host_alloc); false for pageable memory.
+static bool page_locked(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // pageable pointers may set a non-sticky error
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
 }
 
 }  // namespace cg
@@ -114,7 +128,11 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   p.fr0 = bitmaps + words;
   p.fr1 = bitmaps + 2 * words;
   p.fr2 = bitmaps + 3 * words;
-  p.dead = nullptr;  // no per-graph state here: every vertex is scanned
+  // No per-graph state is kept here, so the map of vertices without in-edges
+  // that the handle API builds once is absent: pull rounds load the in-list
+  // offsets of those vertices too (about 10 us more per late pull round at
+  // R-MAT scale 21 than cg_bfs; results are the same).
+  p.dead = nullptr;
   int32_t *queue = reinterpret_cast<int32_t *>(base + kOffQueue);
   p.queue0 = queue;
   p.queue1 = queue + n;
@@ -137,8 +155,7 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   p.unmatched_wait = 0;
   // The array keeps the previous call's contents: the round records and the
   // grid-wait counter must start at zero (bitmaps and outputs are reset by the
-  // kernel itself).
-  CG_CUDA(cudaMemsetAsync(p.ctl, 0, sizeof(BfsCtl), st));
+  // kernel itself); the memset is enqueued below, after the argument checks.
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(512);
@@ -149,11 +166,23 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  CG_CUDA(cudaLaunchKernelEx(&cfg, bfs_persistent, p));
-  if (stats) {
-    CG_CUDA(cudaMemcpyAsync(stats, p.stats, sizeof(cg_stats), cudaMemcpyDeviceToHost, st));
-    CG_CUDA(cudaStreamSynchronize(st));
-    return stats->status;
+  // A call that would wait for the stream cannot run inside a stream capture:
+  // refuse it before anything is enqueued.
+  const bool async_stats = stats && page_locked(stats);
+  if (stats && !async_stats) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CG_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+      set_error_text("cg_bfs_noalloc: pageable stats make the call wait for the stream, and "
+                     "the stream is being captured");
+      return CG_ERR_NOT_SUPPORTED;
+    }
   }
-  return CG_OK;
+  CG_CUDA(cudaMemsetAsync(p.ctl, 0, sizeof(BfsCtl), st));
+  CG_CUDA(cudaLaunchKernelEx(&cfg, bfs_persistent, p));
+  if (!stats) return CG_OK;
+  CG_CUDA(cudaMemcpyAsync(stats, p.stats, sizeof(cg_stats), cudaMemcpyDeviceToHost, st));
+  if (async_stats) return CG_OK;  // valid once the stream has reached this point
+  CG_CUDA(cudaStreamSynchronize(st));
+  return stats->status;
 }

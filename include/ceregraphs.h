@@ -319,10 +319,21 @@ int cg_validate_device(cg_graph *g, const int64_t *roots, int32_t k, const int32
  * rejected with CG_ERR_INVALID_ARG and a message in cg_last_error_string.
  * Every call on a GPU shares the array and it keeps the last call's contents:
  * calls that overlap on that GPU (other streams or threads) race and give
- * wrong results.  The first call on each device sets up the array's device
- * address, so make it before any stream capture.  Direction policy: Beamer's
- * alpha = 15, beta = 18.  With stats != NULL the call waits for `stream` and
- * returns the search's status; with NULL it returns once the work is queued. */
+ * wrong results.  The first call on each device computes the grid size; the
+ * array's device address is looked up on every call.  Direction policy:
+ * Beamer's alpha = 15, beta = 18.  Unlike the handle API it keeps no map of
+ * vertices without in-edges, so late pull rounds are a little slower (about
+ * 10 us per such round at R-MAT scale 21); results are identical.
+ * Outcome of the search (status, rounds, ...):
+ *  - stats in pageable memory: the call waits for `stream` and returns the
+ *    search's status (CG_ERR_NOT_SUPPORTED, before anything is enqueued, if
+ *    the stream is being captured: a wait is not allowed then);
+ *  - stats in page-locked memory (cg_host_alloc, cudaHostAlloc,
+ *    cudaHostRegister): the call returns CG_OK once the work is queued and the
+ *    statistics land in *stats when the stream reaches them -- read
+ *    stats->status after synchronising;
+ *  - stats == NULL: the call returns once the work is queued and a failed
+ *    search (CG_ERR_TIMEOUT, CG_ERR_LEVEL_CAP) is not reported anywhere. */
 #define CG_NOALLOC_MAX_VERTICES (1 << 21)
 #define CG_NOALLOC_MAX_BIG (1 << 20)
 int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off, const int32_t *d_in_idx,

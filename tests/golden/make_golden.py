@@ -299,7 +299,9 @@ def main_loader_only(ref):
 
 if __name__ == "__main__":
   args = [a for a in sys.argv[1:] if not a.startswith("--")]
-  ref_dir = args[0] if args else "/root/reference"
+  if len(args) != 1:
+    sys.exit("usage: make_golden.py REFERENCE_CHECKOUT [--loader-only]")
+  ref_dir = args[0]
   if "--loader-only" in sys.argv:
     main_loader_only(ref_dir)
   else:

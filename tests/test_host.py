@@ -204,22 +204,3 @@ def test_abi_struct_layouts_match_the_header(tmp_path):
     assert got[(cname, "size")] == ctypes.sizeof(cls), cname
     for f, _ in cls._fields_:
       assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
-
-
-def test_integration_notes_structs_match_the_bindings():
-  """The ctypes structs a maintainer copies from INTEGRATION.md have the same
-  fields and size as the package's mirrors, which the layout test checks
-  against the header."""
-  from ceregraphs_gb300 import _lib
-  text = open(os.path.join(ROOT, "INTEGRATION.md"), encoding="utf-8").read()
-  found = 0
-  for name, mirror in (("Stats", _lib.CgStats), ("Options", _lib.CgOptions)):
-    m = re.search(r"class %s\(ctypes\.Structure\):.*?\]\n" % name, text, flags=re.S)
-    assert m, name
-    ns = {"ctypes": ctypes}
-    exec(m.group(0), ns)  # noqa: S102 -- the repository's own documentation
-    cls = ns[name]
-    assert [f for f, _ in cls._fields_] == [f for f, _ in mirror._fields_], name
-    assert ctypes.sizeof(cls) == ctypes.sizeof(mirror), name
-    found += 1
-  assert found == 2
