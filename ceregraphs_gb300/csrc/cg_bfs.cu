@@ -40,11 +40,93 @@ namespace cg {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kPush = 0, kPull = 1;
 constexpr int kBfsBlock = 512;
-// Pull rounds: in-list entries each thread checks before the warp takes over.
-constexpr int kPullThreadScan = 8;
+// Pull rounds: in-list entries a thread loads at once (all in flight before
+// any is tested), and how many entries of its vertex's list a thread scans
+// before the whole warp takes over the rest of it.
+#ifndef CG_PULL_CHUNK
+#define CG_PULL_CHUNK 4
+#endif
+#ifndef CG_PULL_LANE_MAX
+#define CG_PULL_LANE_MAX 32
+#endif
+constexpr int kPullThreadScan = CG_PULL_CHUNK;
+constexpr unsigned kPullLaneMax = CG_PULL_LANE_MAX;
+constexpr int kBfsWarps = kBfsBlock / 32;
 
+// Per-warp shared memory of the bitmap-wide rounds: a staged tile (its words
+// and the exclusive prefix of their popcounts, so that a lane can select the
+// k-th set bit) and the tile's next-frontier words found by a pull round.
+struct __align__(16) WarpTile {  // 16-byte vector accesses to every member
+  uint32_t m[kTileWords];
+  uint32_t pre[kTileWords];
+  uint32_t found[kTileWords];
+};
+static_assert(sizeof(WarpTile) % 16 == 0 && kTileWords % 4 == 0, "16-byte tile rows");
+// Per-warp shared memory of a push round's edge spreading (gather_expand).
+struct WarpExpand {
+  int32_t u[32];
+  int64_t s[32];
+  int64_t x[32];
+};
+__shared__ WarpTile s_tiles[kBfsWarps];
+__shared__ WarpExpand s_expand[kBfsWarps];
+
+__device__ __forceinline__ uint4 ld4(const uint32_t *a) {
+  return *reinterpret_cast<const uint4 *>(a);
+}
+// Non-coherent (read-only path) load: only for data no thread writes while
+// the kernel runs (the dead-vertex map).  Bitmaps that earlier rounds wrote are
+// read with ordinary loads, which the grid waits' acquire makes current.
+__device__ __forceinline__ uint4 ldg4(const uint32_t *a) {
+  return __ldg(reinterpret_cast<const uint4 *>(a));
+}
+__device__ __forceinline__ void st4(uint32_t *a, uint4 v) { *reinterpret_cast<uint4 *>(a) = v; }
+__device__ __forceinline__ bool any4(uint4 v) { return (v.x | v.y | v.z | v.w) != 0u; }
+
+// Bits of word `wi` that stand for vertices < n.
+__device__ __forceinline__ uint32_t valid_bits(int64_t wi, int64_t n) {
+  const int64_t lo = wi * 32;
+  if (lo + 32 <= n) return kFull;
+  if (lo >= n) return 0u;
+  return (1u << (unsigned)(n - lo)) - 1u;
+}
+
+// Stages the tile's 128 words (4 per lane, lane order) in shared memory with
+// the exclusive prefix of their popcounts; returns the tile's total number of
+// set bits (the same in every lane).  All 32 lanes call.
+__device__ __forceinline__ unsigned stage_tile(uint4 m, WarpTile &T) {
+  const int lane = lane_id();
+  const unsigned c0 = __popc(m.x), c1 = __popc(m.y), c2 = __popc(m.z), c3 = __popc(m.w);
+  const unsigned cnt = c0 + c1 + c2 + c3;
+  unsigned incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const unsigned base = incl - cnt;
+  st4(T.m + 4 * lane, m);
+  st4(T.pre + 4 * lane, make_uint4(base, base + c0, base + c0 + c1, base + c0 + c1 + c2));
+  __syncwarp();
+  return __shfl_sync(kFull, incl, 31);
+}
+
+// The k-th set bit (k below the staged total) of the staged tile: word j of
+// the tile and bit b of that word.  The last word whose prefix is <= k holds it.
+__device__ __forceinline__ void select_bit(const WarpTile &T, unsigned k, int &j, int &b) {
+  int lo = 0;
+#pragma unroll
+  for (int step = kTileWords / 2; step > 0; step >>= 1)
+    if (T.pre[lo + step] <= k) lo += step;
+  j = lo;
+  b = (int)__fns(T.m[lo], 0, (int)(k - T.pre[lo]) + 1);
+}
+
+// A thread's discoveries in one round: vertices, and the sum of their
+// out-degrees / in-degrees.  32 bits suffice: a round discovers at most n
+// vertices and their degrees sum to at most nnz < 2^32 (checked at upload).
 struct Acc {
-  unsigned long long nf = 0, mf = 0, visdeg = 0;
+  unsigned nf = 0, mf = 0, visdeg = 0;
 };
 
 // Appends the discoveries of one warp-wide step to the next frontier's queue:
@@ -90,8 +172,8 @@ __device__ __forceinline__ void enqueue_claims(const BfsParams &p, bool claimed,
   }
   if (claimed) {
     acc.nf += 1;
-    acc.mf += (unsigned long long)deg;
-    acc.visdeg += (unsigned long long)deg;
+    acc.mf += (unsigned)deg;
+    acc.visdeg += (unsigned)deg;
   }
 }
 
@@ -173,9 +255,6 @@ __device__ __forceinline__ void gather_expand(const BfsParams &p, const uint32_t
 // Item i goes to warp i first; warps that finish take the rest from a counter.
 __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
                                  RoundRec *Rc, RoundRec *Rn, Acc &acc) {
-  __shared__ int32_t s_u[kBfsBlock / 32][32];
-  __shared__ int64_t s_s[kBfsBlock / 32][32];
-  __shared__ int64_t s_x[kBfsBlock / 32][32];
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -234,8 +313,9 @@ __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32
       }
     } else {
       const unsigned idx = (item - nchunks) * 32u + lane;
-      gather_expand(p, cur, nxt, idx < nlight ? q[idx] : -1, L, next_parity, Rn, acc, s_u[wib],
-                    s_s[wib], s_x[wib]);
+      WarpExpand &X = s_expand[wib];
+      gather_expand(p, cur, nxt, idx < nlight ? q[idx] : -1, L, next_parity, Rn, acc, X.u, X.s,
+                    X.x);
     }
     unsigned nextitem = 0;
     if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
@@ -243,94 +323,204 @@ __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32
   }
 }
 
+// Work items of a bitmap-wide round: (tile, slot) pairs; a tile holds 4096
+// vertices (there are fewer tiles than warps below ~30M vertices) and its S
+// slots split its set bits into S even ranges.  A heavy round (enough work for
+// every warp) hands out about two items per warp, item i to warp i first and
+// the rest from the round record's counter: its work crowds into the low
+// tiles, where the unvisited vertices with in-edges are.  A light round takes
+// S = warps / tiles and item i to warp i, with no counter for the grid's warps
+// to queue on when they all finish at once.
+__device__ __forceinline__ unsigned tile_slots(int64_t tiles, int nwarps, bool heavy) {
+  const int64_t s = heavy ? (2 * (int64_t)nwarps + tiles - 1) / tiles : (int64_t)nwarps / tiles;
+  return (unsigned)(s < 1 ? 1 : (s > 64 ? 64 : s));
+}
+
+__device__ __forceinline__ int64_t next_item(int64_t item, int nwarps, RoundRec *Rc, bool heavy) {
+  if (!heavy) return item + nwarps;
+  unsigned nextitem = 0;
+  if (lane_id() == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
+  return (int64_t)__shfl_sync(kFull, nextitem, 0);
+}
+
 // Push round right after a pull round: the frontier is only in the bitmap, so
-// warps walk its words and expand the set bits 32 at a time.
+// warps stage it a tile at a time (one 16-byte load per lane) and expand its
+// set bits 32 at a time (lane i takes the i-th bit of its batch).
 __device__ void push_round_bitmap(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
-                                  RoundRec *Rn, Acc &acc) {
-  __shared__ int32_t s_u[kBfsBlock / 32][32];
-  __shared__ int64_t s_s[kBfsBlock / 32][32];
-  __shared__ int64_t s_x[kBfsBlock / 32][32];
+                                  RoundRec *Rc, RoundRec *Rn, bool heavy, Acc &acc) {
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int next_parity = (L + 1) & 1;
-  for (int64_t w = warp_id_global(); w < p.words; w += nwarps) {
-    const uint32_t bits = cur[w];
-    if (!bits) continue;
-    const int32_t u = ((bits >> lane) & 1u) ? (int32_t)(w * 32 + lane) : -1;
-    gather_expand(p, cur, nxt, u, L, next_parity, Rn, acc, s_u[wib], s_s[wib], s_x[wib]);
+  WarpTile &T = s_tiles[wib];
+  WarpExpand &X = s_expand[wib];
+  const unsigned S = tile_slots(p.tiles, nwarps, heavy);
+  const int64_t items = p.tiles * S;
+  for (int64_t item = warp_id_global(); item < items; item = next_item(item, nwarps, Rc, heavy)) {
+    const int64_t t = item % p.tiles;
+    const unsigned slot = (unsigned)(item / p.tiles);
+    const uint4 c = ld4(cur + t * kTileWords + 4 * lane);
+    const unsigned total = stage_tile(c, T);
+    const unsigned k1 = (unsigned)((unsigned long long)total * (slot + 1) / S);
+    for (unsigned b = (unsigned)((unsigned long long)total * slot / S); b < k1; b += 32) {
+      int32_t u = -1;
+      if (b + lane < k1) {
+        int j, bit;
+        select_bit(T, b + lane, j, bit);
+        u = (int32_t)((t * kTileWords + j) * 32 + bit);
+      }
+      gather_expand(p, cur, nxt, u, L, next_parity, Rn, acc, X.u, X.s, X.x);
+    }
+    __syncwarp();  // T is restaged by the next item
   }
 }
 
 // Bottom-up round: every unvisited vertex scans its ascending in-list and
-// stops at the first source in F_L.  One warp owns one bitmap word (so the
-// next-frontier word is written whole, without atomics); each lane checks the
-// first kPullThreadScan sources itself, longer remainders are scanned by the
-// whole warp, 32 sources a step, one vertex at a time.
-__device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
-                           Acc &acc) {
+// stops at the first source in F_L, which is its lowest-index parent.
+// Work items are (tile, slot) pairs of 4096-vertex bitmap tiles: one 16-byte
+// load per lane of each of vis, F_L and the map of vertices without in-edges
+// gives the tile's unvisited set, staged in shared memory, and the slot takes
+// an even range of it.  Each lane works on one vertex of the range at a time,
+// kPullThreadScan entries of its list a step (all loads in flight before any
+// test); a lane whose vertex is done (found, or its list exhausted) takes the
+// range's next vertex at once, so lanes do not wait for the slowest list of a
+// batch.  A list still unresolved after kPullLaneMax entries is finished by
+// the whole warp, 32 entries a step.  Found vertices set their bit in the
+// warp's shared copy of the tile's next-frontier words, ORed into F_{L+1} at
+// the end of the item.  Slot 0 of each tile also merges F_L into vis (the
+// union vis | F_L that other slots test is unchanged by it) and clears F_{L-1}
+// (the next round's output bitmap), so pull rounds need no sweep.
+__device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, uint32_t *old,
+                           int L, RoundRec *Rc, bool heavy, Acc &acc) {
   const int lane = lane_id();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int wib = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = warp_id_global(); w < p.words; w += nwarps) {
-    const uint32_t seen = p.vis[w] | cur[w] | (p.dead ? p.dead[w] : 0u);
-    const int64_t v = w * 32 + lane;
-    const bool active = v < p.n && !((seen >> lane) & 1u);
-    if (__ballot_sync(kFull, active) == 0) continue;
-    bool found = false;
-    int64_t s = 0, e = 0;
-    if (active) {
-      s = __ldg(p.in_off + v);
-      e = __ldg(p.in_off + v + 1);
-      // the first kPullThreadScan sources: all loads issued before any test
-      int32_t u[kPullThreadScan];
-      uint32_t hit = 0;
-#pragma unroll
-      for (int k = 0; k < kPullThreadScan; ++k) u[k] = s + k < e ? __ldg(p.in_idx + s + k) : -1;
-#pragma unroll
-      for (int k = 0; k < kPullThreadScan; ++k)
-        if (u[k] >= 0 && ((cur[(uint32_t)u[k] >> 5] >> (u[k] & 31)) & 1u)) hit |= 1u << k;
-      if (hit) {
-        const int k = __ffs(hit) - 1;  // ascending list: the lowest hit is the minimum
-        int32_t uk = u[0];
-#pragma unroll
-        for (int t = 1; t < kPullThreadScan; ++t)
-          if (t == k) uk = u[t];
-        p.parents[v] = uk;
-        p.levels[v] = L + 1;
-        found = true;
-      }
+  WarpTile &T = s_tiles[wib];
+  const unsigned S = tile_slots(p.tiles, nwarps, heavy);
+  const int64_t items = p.tiles * S;
+  for (int64_t item = warp_id_global(); item < items; item = next_item(item, nwarps, Rc, heavy)) {
+    const int64_t t = item % p.tiles;
+    const unsigned slot = (unsigned)(item / p.tiles);
+    const int64_t w0 = t * kTileWords + 4 * lane;
+    const uint4 vi = ld4(p.vis + w0);
+    const uint4 cu = ld4(cur + w0);
+    uint4 dd;
+    if (p.dead) {
+      dd = ldg4(p.dead + w0);
+    } else {
+      dd = make_uint4(~valid_bits(w0, p.n), ~valid_bits(w0 + 1, p.n), ~valid_bits(w0 + 2, p.n),
+                      ~valid_bits(w0 + 3, p.n));
     }
-    unsigned rest = __ballot_sync(kFull, active && !found && e > s + kPullThreadScan);
-    while (rest) {
-      const int j = __ffs(rest) - 1;
-      rest &= rest - 1;
-      const int64_t sj = __shfl_sync(kFull, s, j) + kPullThreadScan;
-      const int64_t ej = __shfl_sync(kFull, e, j);
-      for (int64_t base = sj; base < ej; base += 32) {
-        const int64_t i = base + lane;
-        int32_t u = 0;
-        bool hit = false;
-        if (i < ej) {
-          u = __ldg(p.in_idx + i);
-          hit = (cur[(uint32_t)u >> 5] >> (u & 31)) & 1u;
-        }
-        const unsigned who = __ballot_sync(kFull, hit);
-        if (who) {
-          if (lane == __ffs(who) - 1) {
-            p.parents[w * 32 + j] = u;
-            p.levels[w * 32 + j] = L + 1;
+    if (slot == 0) {
+      if (any4(cu))
+        st4(p.vis + w0, make_uint4(vi.x | cu.x, vi.y | cu.y, vi.z | cu.z, vi.w | cu.w));
+      st4(old + w0, make_uint4(0u, 0u, 0u, 0u));
+    }
+    const uint4 un = make_uint4(~(vi.x | cu.x | dd.x), ~(vi.y | cu.y | dd.y),
+                                ~(vi.z | cu.z | dd.z), ~(vi.w | cu.w | dd.w));
+    st4(T.found + 4 * lane, make_uint4(0u, 0u, 0u, 0u));
+    const unsigned total = stage_tile(un, T);
+    const unsigned k1 = (unsigned)((unsigned long long)total * (slot + 1) / S);
+    unsigned cursor = (unsigned)((unsigned long long)total * slot / S);
+    // lane state: the vertex it works on (v, word j / bit of the tile), its
+    // list [s, s + deg) and the next entry to scan
+    bool has = false;
+    int j = 0, bit = 0;
+    int64_t s = 0;
+    unsigned deg = 0, pos = 0;
+    const int64_t v0 = t * kTileWords * 32;  // the tile's first vertex
+    bool refill = true;  // some lane has no vertex (warp-uniform)
+    while (true) {
+      if (refill) {
+        const unsigned need = __ballot_sync(kFull, !has);
+        if (!has) {
+          const unsigned k = cursor + __popc(need & lt_mask);
+          if (k < k1) {
+            has = true;
+            select_bit(T, k, j, bit);
+            const int64_t v = v0 + j * 32 + bit;
+            s = __ldg(p.in_off + v);
+            deg = (unsigned)(__ldg(p.in_off + v + 1) - s);
+            pos = 0;
           }
-          if (lane == j) found = true;
-          break;
+        }
+        cursor += __popc(need);
+      }
+      if (!__any_sync(kFull, has)) break;
+      bool found = false;
+      if (has && pos < kPullLaneMax) {
+        int32_t u[kPullThreadScan];
+#pragma unroll
+        for (int k = 0; k < kPullThreadScan; ++k)
+          u[k] = pos + k < deg ? __ldg(p.in_idx + s + pos + k) : -1;
+        uint32_t hit = 0;
+#pragma unroll
+        for (int k = 0; k < kPullThreadScan; ++k)
+          if (u[k] >= 0 && ((cur[(uint32_t)u[k] >> 5] >> (u[k] & 31)) & 1u)) hit |= 1u << k;
+        if (hit) {
+          const int k = __ffs(hit) - 1;  // ascending list: the lowest hit is the minimum
+          int32_t uk = u[0];
+#pragma unroll
+          for (int q = 1; q < kPullThreadScan; ++q)
+            if (q == k) uk = u[q];
+          const int64_t v = v0 + j * 32 + bit;
+          p.parents[v] = uk;
+          p.levels[v] = L + 1;
+          found = true;
+        }
+        pos += kPullThreadScan;
+      }
+      // lists still open after kPullLaneMax entries: the whole warp scans the
+      // rest, one vertex at a time
+      unsigned rest = __ballot_sync(kFull, has && !found && pos >= kPullLaneMax && pos < deg);
+      while (rest) {
+        const int jl = __ffs(rest) - 1;
+        rest &= rest - 1;
+        const int64_t sj = __shfl_sync(kFull, s, jl);
+        const unsigned pj = __shfl_sync(kFull, pos, jl);
+        const unsigned dj = __shfl_sync(kFull, deg, jl);
+        const int64_t vj = v0 + __shfl_sync(kFull, j * 32 + bit, jl);
+        bool got = false;
+        for (unsigned base = pj; base < dj; base += 32) {
+          const unsigned i = base + lane;
+          int32_t u = 0;
+          bool hit = false;
+          if (i < dj) {
+            u = __ldg(p.in_idx + sj + i);
+            hit = (cur[(uint32_t)u >> 5] >> (u & 31)) & 1u;
+          }
+          const unsigned who = __ballot_sync(kFull, hit);
+          if (who) {
+            if (lane == __ffs(who) - 1) {
+              p.parents[vj] = u;
+              p.levels[vj] = L + 1;
+            }
+            got = true;
+            break;
+          }
+        }
+        if (lane == jl) {
+          found = got;
+          pos = deg;  // scanned to the end (or found)
         }
       }
+      if (found) {
+        atomicOr(&T.found[j], 1u << bit);
+        acc.nf += 1;
+        acc.visdeg += deg;
+      }
+      const bool done = has && (found || pos >= deg);
+      if (done) has = false;
+      refill = __any_sync(kFull, done) && cursor < k1;
     }
-    const unsigned m = __ballot_sync(kFull, found);
-    if (lane == 0 && m) nxt[w] = m;
-    if (found) {
-      acc.nf += 1;
-      acc.visdeg += (unsigned long long)(e - s);
-    }
+    __syncwarp();
+    const uint4 f = ld4(T.found + 4 * lane);
+    if (f.x) atomicOr(nxt + w0, f.x);
+    if (f.y) atomicOr(nxt + w0 + 1, f.y);
+    if (f.z) atomicOr(nxt + w0 + 2, f.z);
+    if (f.w) atomicOr(nxt + w0 + 3, f.w);
+    __syncwarp();  // T is restaged by the next item
   }
 }
 
@@ -395,97 +585,117 @@ __device__ __forceinline__ int next_direction(const BfsParams &p, int dir, unsig
   }
 }
 
-// Payload of a round's grid-wide wait.
-constexpr unsigned kDone = 1u, kNextPull = 2u;
+// Payload of a round's grid-wide barrier: the search ended; the next round
+// pulls; the next round is heavy (enough work for every warp of the grid).
+constexpr unsigned kDone = 1u, kNextPull = 2u, kHeavy = 4u;
 
-// End of round L, run by the block that arrives last (it sees every block's
-// counters): the termination test of bool_pe.csl:1048-1100 (nf == 0 ends the
-// search), the direction for round L + 1, the statistics, and the reset of
-// the round record that round L + 1 accumulates into next.
-__device__ unsigned decide_round(const BfsParams &p, int L, int dir) {
-  BfsCtl *ctl = p.ctl;
-  const RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
-  // every load first (from L2: other blocks wrote these), so that they are in
-  // flight together -- this function runs while the whole grid waits
-  unsigned long long nfs[kCounterShards], mfs[kCounterShards], vds[kCounterShards];
-#pragma unroll
-  for (int i = 0; i < kCounterShards; ++i) {
-    nfs[i] = __ldcg(&Rn->nf[i]);
-    mfs[i] = __ldcg(&Rn->mf[i]);
-    vds[i] = __ldcg(&Rn->visdeg[i]);
+// Flat grid-wide barrier of the per-root kernel, called by thread 0 of each
+// block after a __syncthreads: one fire-and-forget release add on the launch's
+// 64-bit arrival count, relaxed polls until the count reaches `target` (the
+// b-th barrier of a launch waits for (b + 1) * gridDim.x arrivals; the count is
+// zeroed before every launch), then one acquire fence, which makes every
+// block's writes before its arrival visible.  Relaxed polls leave the SM's L1
+// alone (an acquire load invalidates it while blocks of the same SM may still
+// be working).  Bounded: after timeout_ns, or once another block has flagged
+// an error, the thread records CG_ERR_TIMEOUT and returns false, so a barrier
+// that cannot complete ends the kernel instead of spinning.
+__device__ __forceinline__ bool flat_barrier(unsigned long long *count, unsigned long long target,
+                                             int *status, long long timeout_ns) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(count) : "memory");
+  long long t0 = 0;
+  unsigned spins = 0;
+  while (true) {
+    unsigned long long c;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(c) : "l"(count) : "memory");
+    if (c >= target) break;
+    if ((++spins & 255u) == 0) {
+      if (t0 == 0) t0 = global_ns();
+      if (*(volatile int *)status != 0 || global_ns() - t0 > timeout_ns) {
+        atomicCAS(status, 0, (int)CG_ERR_TIMEOUT);
+        return false;
+      }
+    }
   }
-  const long long t_round = __ldcg(&ctl->t_round);
-  const int pull_rounds = __ldcg(&ctl->pull_rounds);
-  const int switches = __ldcg(&ctl->switches);
-  const unsigned long long visited = __ldcg(&ctl->visited);
-  const unsigned long long prev_nf = __ldcg(&ctl->prev_nf);
-  const unsigned long long explored = __ldcg(&ctl->explored);
-  const int status = __ldcg(&ctl->status);
-  unsigned long long nf = 0, mf = 0, vd = 0;
-#pragma unroll
-  for (int i = 0; i < kCounterShards; ++i) {
-    nf += nfs[i];
-    mf += mfs[i];
-    vd += vds[i];
-  }
-  cg_stats *st = p.stats;
-  const long long now = global_ns();
-  if (L < CG_HISTORY) {
-    st->nf_history[L] = (int64_t)nf;
-    st->direction_history[L] = dir;
-    st->round_ns[L] = now - t_round;
-  }
-  ctl->t_round = now;
-  const int pulls = pull_rounds + (dir == kPull ? 1 : 0);
-  ctl->pull_rounds = pulls;
-  const unsigned long long vis_total = visited + nf;
-  ctl->visited = vis_total;
-  bool done = nf == 0;
-  int stat = status;
-  if (!done && L + 1 >= p.level_cap) {
-    atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
-    if (stat == 0) stat = CG_ERR_LEVEL_CAP;
-    done = true;
-  }
-  const int next = next_direction(p, dir, nf, prev_nf, mf, explored);
-  ctl->explored = explored + vd;
-  ctl->prev_nf = nf;
-  const int sw = switches + ((!done && next != dir) ? 1 : 0);
-  ctl->switches = sw;
-  RoundRec *Rz = &ctl->rec[(L + 2) % kRing];  // last used in round L - 2
-  for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->mf[i] = Rz->visdeg[i] = 0;
-  Rz->big = 0;
-  Rz->nlight = Rz->work = 0;
-  if (done) {
-    const int rounds = L + 1;
-    st->status = stat;
-    st->rounds = rounds;
-    st->visited = (int64_t)vis_total;
-    st->pull_rounds = pulls;
-    st->switches = sw;
-    st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
-    st->finish_ns = 0;
-    st->device_ms = 0.f;
-  }
-  return (done ? kDone : 0u) | (next == kPull ? kNextPull : 0u);
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  return true;
 }
 
-struct RoundDecision {
-  const BfsParams *p;
-  int L, dir;
-  __device__ unsigned operator()() const { return decide_round(*p, L, dir); }
+// The search-wide bookkeeping of bool_pe.csl:947-1100 (visited total,
+// explored edges, previous frontier size, pull rounds, direction switches).
+// Every block keeps its own copy (thread 0) and updates it from the same round
+// totals, so all blocks take the same decision without a second barrier.
+struct SearchState {
+  unsigned long long visited, prev_nf, explored;
+  int pull_rounds, switches;
+  long long t_mark;  // block 0: end of the previous round on the device clock
 };
 
-struct SetupDecision {
-  BfsCtl *ctl;
-  cg_stats *st;
-  __device__ unsigned operator()() const {
-    const long long now = global_ns();
-    st->setup_ns = now - ctl->t_start;
-    ctl->t_round = now;
-    return 0u;
+// End of round L in warp 0 of every block, after the round's barrier: the
+// termination test of bool_pe.csl:1048-1100 (nf == 0 ends the search) and the
+// direction of round L + 1.  Lanes 0-23 each load one sharded counter of the
+// round record (one L2 round trip), lane 0 takes the decision and block 0's
+// lane 0 records the round's statistics.  All 32 lanes call; lane 0's return
+// value is the payload.
+__device__ unsigned round_decision(const BfsParams &p, int L, int dir, SearchState &ss) {
+  BfsCtl *ctl = p.ctl;
+  const RoundRec *Rn = &ctl->rec[(L + 1) % kRing];
+  const int lane = lane_id();
+  const int g = lane >> 3, sh = lane & (kCounterShards - 1);
+  static_assert(kCounterShards == 8, "three groups of eight lanes");
+  unsigned long long x = 0;
+  if (g == 0) x = __ldcg(&Rn->nf[sh]);
+  else if (g == 1) x = __ldcg(&Rn->mf[sh]);
+  else if (g == 2) x = __ldcg(&Rn->visdeg[sh]);
+#pragma unroll
+  for (int o = 1; o < kCounterShards; o <<= 1) x += __shfl_xor_sync(kFull, x, o);
+  const unsigned long long nf = __shfl_sync(kFull, x, 0);
+  const unsigned long long mf = __shfl_sync(kFull, x, 8);
+  const unsigned long long vd = __shfl_sync(kFull, x, 16);
+  if (lane != 0) return 0u;
+  const bool block0 = blockIdx.x == 0;
+  ss.pull_rounds += dir == kPull ? 1 : 0;
+  ss.visited += nf;
+  bool done = nf == 0;
+  bool capped = false;
+  if (!done && L + 1 >= p.level_cap) {
+    capped = true;
+    done = true;
   }
-};
+  const int next = next_direction(p, dir, nf, ss.prev_nf, mf, ss.explored);
+  ss.explored += vd;
+  ss.prev_nf = nf;
+  ss.switches += (!done && next != dir) ? 1 : 0;
+  if (block0) {
+    cg_stats *st = p.stats;
+    const long long now = global_ns();
+    if (L < CG_HISTORY) {
+      st->nf_history[L] = (int64_t)nf;
+      st->direction_history[L] = dir;
+      st->round_ns[L] = now - ss.t_mark;
+    }
+    ss.t_mark = now;
+    if (capped) atomicCAS(&ctl->status, 0, (int)CG_ERR_LEVEL_CAP);
+    if (done) {
+      const int rounds = L + 1;
+      const int stat = *(volatile int *)&ctl->status;
+      st->status = stat != 0 ? stat : (capped ? (int)CG_ERR_LEVEL_CAP : 0);
+      st->rounds = rounds;
+      st->visited = (int64_t)ss.visited;
+      st->pull_rounds = ss.pull_rounds;
+      st->switches = ss.switches;
+      st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
+      st->finish_ns = 0;
+      st->device_ms = 0.f;
+    }
+  }
+  // a pull round's work is the unvisited vertices with in-edges, a push
+  // round's (from the bitmap) its frontier
+  const unsigned long long work =
+      next == kPull ? (p.live > (int64_t)ss.visited ? (unsigned long long)p.live - ss.visited : 0ull)
+                    : nf;
+  const bool heavy = work >= 32ull * (unsigned long long)((gridDim.x * blockDim.x) >> 5);
+  return (done ? kDone : 0u) | (next == kPull ? kNextPull : 0u) | (heavy ? kHeavy : 0u);
+}
 
 // A host caller's outputs, copied by every block into the page-locked
 // buffers (16 bytes a thread when n allows).  Kept out of line so the search
@@ -516,16 +726,26 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 
   // ---- phase 0: start_spmv -- reset outputs and bitmaps, seed the root ----
-  if (leader) ctl->t_start = global_ns();
+  __shared__ SearchState ss;  // thread 0's copy of the search-wide bookkeeping
+  if (leader) ss.t_mark = global_ns();
   for (int64_t i = gtid; i < p.n; i += nthreads) {
     p.levels[i] = (i == root) ? 0 : -1;
     p.parents[i] = (i == root) ? root : -1;
   }
-  for (int64_t w = gtid; w < p.words; w += nthreads) {
-    p.vis[w] = 0;
-    p.fr0[w] = (w == (root >> 5)) ? (1u << (root & 31)) : 0u;
-    p.fr1[w] = 0;
-    p.fr2[w] = 0;
+  // whole tiles (the padding past `words` too: a bitmap-wide round reads it)
+  const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
+  const int64_t root_word = root >> 5;
+  for (int64_t i = gtid; i < p.tiles * (kTileWords / 4); i += nthreads) {
+    st4(p.vis + 4 * i, zero4);
+    uint4 f0 = zero4;
+    if (i == (root_word >> 2)) {  // F_0 = {root}, seeded by the thread that clears its word
+      const uint32_t bit = 1u << (root & 31);
+      const int c = (int)(root_word & 3);
+      f0 = make_uint4(c == 0 ? bit : 0u, c == 1 ? bit : 0u, c == 2 ? bit : 0u, c == 3 ? bit : 0u);
+    }
+    st4(p.fr0 + 4 * i, f0);
+    st4(p.fr1 + 4 * i, zero4);
+    st4(p.fr2 + 4 * i, zero4);
   }
   if (leader) {
     const int64_t deg = p.out_off[root + 1] - p.out_off[root];
@@ -533,9 +753,6 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
     R0->nf[0] = 1;
     R0->mf[0] = deg;
     R0->visdeg[0] = deg;
-    ctl->visited = 1;
-    ctl->prev_nf = 1;
-    ctl->explored = (unsigned long long)deg;
     if (deg <= kLightMax) {
       p.queue0[0] = root;
       R0->nlight = 1;
@@ -545,19 +762,33 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
       R0->big = (1ull << 32) | (unsigned long long)deg;
     }
   }
-  // the sync word's generation, read before this block's first arrival (it
-  // cannot advance before then); every completed wait adds one
-  unsigned gen = 0;
-  if (threadIdx.x == 0) gen = (unsigned)ld_acquire64(&ctl->wait.sync);
+  // barrier b of this launch completes at (b + 1) * gridDim.x arrivals
+  __shared__ unsigned long long s_target;
   __syncthreads();
-  if (threadIdx.x == 0)
-    s_payload = arrive_and_wait_gen(&ctl->wait, gen++, &ctl->status, p.timeout_ns,
-                                    p.unmatched_wait ? 1u : 0u, SetupDecision{ctl, p.stats});
+  if (threadIdx.x == 0) {
+    const unsigned long long target = gridDim.x;
+    s_target = target;
+    // the test hook expects one arrival more than the grid has: it must time out
+    const bool ok0 = flat_barrier(&ctl->arrive, target + (p.unmatched_wait ? 1u : 0u),
+                                  &ctl->status, p.timeout_ns);
+    ss.visited = 1;
+    ss.prev_nf = 1;
+    ss.explored = (unsigned long long)(__ldg(p.out_off + root + 1) - __ldg(p.out_off + root));
+    ss.pull_rounds = 0;
+    ss.switches = 0;
+    if (blockIdx.x == 0 && ok0) {
+      const long long now = global_ns();
+      p.stats->setup_ns = now - ss.t_mark;
+      ss.t_mark = now;
+    }
+    s_payload = ok0 ? 0u : kWaitFailed;
+  }
   __syncthreads();
   bool ok = s_payload != kWaitFailed;
 
   uint32_t *fr0 = p.fr0, *fr1 = p.fr1, *fr2 = p.fr2;
   int dir = kPush;
+  bool heavy = false;
   bool queued = true;  // F_L is in a queue (a pull round leaves it in the bitmap only)
   int L = 0;
   Acc acc;
@@ -571,32 +802,54 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
       if (queued)
         push_round_queue(p, cur, nxt, L, Rc, Rn, acc);
       else
-        push_round_bitmap(p, cur, nxt, L, Rn, acc);
+        push_round_bitmap(p, cur, nxt, L, Rc, Rn, heavy, acc);
+      // vis |= F_L (readers test vis | F_L, so this races with nothing) and
+      // clear F_{L-1}, which becomes the next round's output bitmap; a pull
+      // round does both in its own tile pass
+      for (int64_t i = gtid; i < p.tiles * (kTileWords / 4); i += nthreads) {
+        const uint4 c = ld4(cur + 4 * i);
+        if (any4(c)) {
+          const uint4 vv = ld4(p.vis + 4 * i);
+          st4(p.vis + 4 * i, make_uint4(vv.x | c.x, vv.y | c.y, vv.z | c.z, vv.w | c.w));
+        }
+        st4(old + 4 * i, zero4);
+      }
     } else {
-      pull_round(p, cur, nxt, L, acc);
-    }
-    // vis |= F_L (readers test vis | F_L, so this races with nothing) and
-    // clear F_{L-1}, which becomes the next round's output bitmap
-    for (int64_t w = gtid; w < p.words; w += nthreads) {
-      const uint32_t c = cur[w];
-      if (c) p.vis[w] |= c;
-      old[w] = 0;
+      pull_round(p, cur, nxt, old, L, Rc, heavy, acc);
     }
     unsigned long long a, b, c;
     block_totals(acc, a, b, c);
-    if (threadIdx.x == 0) {
-      const int sh = blockIdx.x % kCounterShards;
-      if (a) atomicAdd(&Rn->nf[sh], a);
-      if (b) atomicAdd(&Rn->mf[sh], b);
-      if (c) atomicAdd(&Rn->visdeg[sh], c);
-      s_payload = arrive_and_wait_gen(&ctl->wait, gen++, &ctl->status, p.timeout_ns, 0u,
-                                      RoundDecision{&p, L, dir});
+    if (threadIdx.x < 32) {
+      bool arrived = false;
+      if (threadIdx.x == 0) {
+        const int sh = blockIdx.x % kCounterShards;
+        if (a) atomicAdd(&Rn->nf[sh], a);
+        if (b) atomicAdd(&Rn->mf[sh], b);
+        if (c) atomicAdd(&Rn->visdeg[sh], c);
+        if (blockIdx.x == 0) {
+          // the record round L + 1 accumulates into next: its last readers were
+          // done before the barrier of round L - 2 (ordered by this arrival)
+          RoundRec *Rz = &ctl->rec[(L + 2) % kRing];
+          for (int i = 0; i < kCounterShards; ++i) Rz->nf[i] = Rz->mf[i] = Rz->visdeg[i] = 0;
+          Rz->big = 0;
+          Rz->nlight = Rz->work = 0;
+        }
+        const unsigned long long target = s_target + gridDim.x;
+        s_target = target;
+        arrived = flat_barrier(&ctl->arrive, target, &ctl->status, p.timeout_ns);
+      }
+      // lane 0's acquire fence, then this warp barrier, order the other lanes'
+      // counter loads after every block's arrival
+      arrived = __shfl_sync(kFull, arrived, 0);
+      const unsigned payload = arrived ? round_decision(p, L, dir, ss) : kWaitFailed;
+      if (threadIdx.x == 0) s_payload = payload;
     }
     __syncthreads();
     const unsigned payload = s_payload;
     if (payload == kWaitFailed || (payload & kDone)) break;
     queued = dir == kPush;  // a push round queued F_{L+1}; a pull round did not
     dir = (payload & kNextPull) ? kPull : kPush;
+    heavy = (payload & kHeavy) != 0;
     uint32_t *t = fr2;  // rotate: F_{L+1} becomes the frontier
     fr2 = fr0;
     fr0 = fr1;
@@ -643,8 +896,19 @@ int64_t bfs_big_capacity(int64_t n, int64_t nnz) {
   return c < n ? c : n;
 }
 
+// Vertices with in-edges: n minus the dead bits below n.
+__global__ void live_count_kernel(int64_t n, int64_t words, const uint32_t *__restrict__ dead,
+                                  unsigned long long *live) {
+  unsigned long long c = 0;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (int64_t)gridDim.x * blockDim.x)
+    c += (unsigned long long)__popc(~dead[w] & valid_bits(w, n));
+  c = warp_sum(c);
+  if (lane_id() == 0 && c) atomicAdd(live, c);
+}
+
 // Bit v of dead[v / 32]: vertex v has no in-edges, so no round reaches it
-// (bits past n are set too).
+// (bits past n are set too, through the tile padding: `words` = stride).
 __global__ void dead_map_kernel(int64_t n, int64_t words, const int64_t *__restrict__ in_off,
                                 uint32_t *dead) {
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
@@ -693,25 +957,36 @@ static int setup_wait(cudaStream_t s) {
 
 int dead_prepare(cg_graph *g) {
   if (g->dead) return CG_OK;
-  const int64_t words = (g->n + 31) / 32;
+  const int64_t words = bitmap_stride(g->n);
   uint32_t *dead = nullptr;
-  if (cudaMalloc(&dead, sizeof(uint32_t) * (size_t)words) != cudaSuccess)
+  unsigned long long *d_live = nullptr;  // the live count, read back once
+  if (cudaMalloc(&dead, sizeof(uint32_t) * (size_t)words) != cudaSuccess ||
+      cudaMalloc(&d_live, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaFree(dead);
     return CG_ERR_OUT_OF_MEMORY;
+  }
+  unsigned long long live = 0;
   cudaStream_t s = nullptr;
   int rc = setup_stream(g, &s);
   if (!rc) {
     const int64_t blocks = (words + 255) / 256;
-    dead_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(g->n, words,
-                                                                               g->in_off, dead);
-    const cudaError_t e = cudaGetLastError();
+    const unsigned grid = (unsigned)(blocks < 4096 ? blocks : 4096);
+    cudaError_t e = cudaMemsetAsync(d_live, 0, sizeof(unsigned long long), s);
+    dead_map_kernel<<<grid, 256, 0, s>>>(g->n, words, g->in_off, dead);
+    live_count_kernel<<<grid, 256, 0, s>>>(g->n, words, dead, d_live);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&live, d_live, sizeof(live), cudaMemcpyDeviceToHost, s);
     rc = setup_wait(s);
     if (!rc && e != cudaSuccess) rc = cuda_fail(e, "dead-vertex map");
   }
+  cudaFree(d_live);
   if (rc) {
     cudaFree(dead);
     return rc;
   }
   g->dead = dead;
+  g->live = (int64_t)live;
   g->device_bytes += sizeof(uint32_t) * words;
   return CG_OK;
 }
@@ -725,7 +1000,7 @@ int bfs_prepare(cg_graph *g) {
   if (!dev_coop) return CG_ERR_NOT_SUPPORTED;
   const int64_t words = (g->n + 31) / 32;
   const int64_t bcap = bfs_big_capacity(g->n, g->nnz);
-  const size_t bytes_bm = sizeof(uint32_t) * 4 * (size_t)words;
+  const size_t bytes_bm = sizeof(uint32_t) * 4 * (size_t)bitmap_stride(g->n);
   const size_t bytes_q = sizeof(int32_t) * 2 * (size_t)g->n;
   const size_t bytes_b = sizeof(uint32_t) * 2 * (size_t)bcap;
   uint32_t *bitmaps = nullptr, *bigoff = nullptr;
@@ -793,15 +1068,18 @@ int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents,
   p.n = g->n;
   p.nnz = g->nnz;
   p.words = g->words;
+  const int64_t stride = bitmap_stride(g->n);
+  p.tiles = stride / kTileWords;
   p.in_off = g->in_off;
   p.in_idx = g->in_idx;
   p.out_off = g->out_off;
   p.out_idx = g->out_idx;
   p.vis = g->bitmaps;
-  p.fr0 = g->bitmaps + g->words;
-  p.fr1 = g->bitmaps + 2 * g->words;
-  p.fr2 = g->bitmaps + 3 * g->words;
+  p.fr0 = g->bitmaps + stride;
+  p.fr1 = g->bitmaps + 2 * stride;
+  p.fr2 = g->bitmaps + 3 * stride;
   p.dead = g->dead;
+  p.live = g->live;
   p.queue0 = g->queue;
   p.queue1 = g->queue + g->n;
   p.bigoff0 = g->bigoff;

@@ -5,12 +5,14 @@
 //   out_off int64[n+1], out_idx int32[nnz]   CSC of A (column c = targets of c);
 //                                             aliases of in_* when A is symmetric
 // Per-root search state (allocated once per handle, reused by every search):
-//   vis, fr[3]     uint32[words]  packed bitmaps: visited-before-the-frontier and three
+//   vis, fr[3]     uint32[stride] packed bitmaps: visited-before-the-frontier and three
 //                                 rotating frontier bitmaps (round L reads fr[L%3] = F_L,
 //                                 writes fr[(L+1)%3] and clears fr[(L+2)%3]); a vertex
 //                                 counts as visited when its bit is in vis | F_L.  These
 //                                 are the reference's visited_bitmap / x_bitmap / y_bitmap
-//                                 (bool_pe.csl) over all n vertices instead of per PE
+//                                 (bool_pe.csl) over all n vertices instead of per PE.
+//                                 stride = words rounded up to whole tiles of kTileWords
+//                                 (16-byte vector loads; the padding stays zero)
 //   queue[2]       int32[n]       push-round frontier queues: light vertices (out-degree
 //                                 <= kLightMax) from the front, big ones from the back
 //   bigoff[2]      uint32[bcap]   prefix offsets of the big vertices' edge lists, in
@@ -54,6 +56,13 @@ constexpr int kPushChunk = 1024;  // edges of big frontier vertices per work ite
 
 constexpr int kRing = 4;          // per-round record ring (rounds L .. L+3)
 
+// Bitmap words a warp stages per tile of a bitmap-wide round (4 per lane, one
+// 16-byte load each): 4096 vertices.  Bitmaps are allocated in whole tiles.
+constexpr int kTileWords = 128;
+__host__ __device__ constexpr int64_t bitmap_stride(int64_t n) {
+  return ((n + 31) / 32 + kTileWords - 1) / kTileWords * kTileWords;
+}
+
 // Statistics of frontier F_k (the vertices at level k) and the queue holding it.
 struct RoundRec {
   unsigned long long nf[kCounterShards];      // |F_k|
@@ -65,32 +74,28 @@ struct RoundRec {
   unsigned long long pad[6];
 };
 
-// Only the block that arrives last at a round's grid-wide wait reads and
-// writes the round bookkeeping (prev_nf .. t_round); the waits order these
-// accesses from round to round.
+// Control block of one per-root search, zeroed before every launch.  The
+// search-wide bookkeeping (visited total, explored edges, ...) is not here:
+// every block keeps its own copy, updated from the same round totals.
 struct BfsCtl {
-  GridWait wait;               // own 128-byte lines
-  int status;
-  int pull_rounds;
-  int switches;
-  int pad0;
-  unsigned long long visited;
-  unsigned long long prev_nf;
-  unsigned long long explored;
-  long long t_start;
-  long long t_round;
-  unsigned long long pad[9];
+  unsigned long long arrive;   // flat grid barrier: arrivals so far in this launch
+  unsigned long long pad0[15];
+  int status;                  // first error (CG_ERR_TIMEOUT, CG_ERR_LEVEL_CAP), else 0
+  int pad1[31];
   RoundRec rec[kRing];
 };
 
 struct BfsParams {
   int64_t n, nnz, words;
+  int64_t tiles;         // bitmap tiles: stride / kTileWords
   const int64_t *__restrict__ in_off;
   const int32_t *__restrict__ in_idx;
   const int64_t *__restrict__ out_off;
   const int32_t *__restrict__ out_idx;
   uint32_t *vis, *fr0, *fr1, *fr2;
-  const uint32_t *dead;  // vertices without in-edges (never reached), or null
+  const uint32_t *dead;  // vertices without in-edges (never reached), or null; bits
+                         // past n are set, `stride` words
+  int64_t live;          // vertices with in-edges (n when `dead` is null)
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   int32_t *levels, *parents;
@@ -126,9 +131,11 @@ struct cg_graph {
   cudaStream_t stream = nullptr;
   cg_options opt{};
   // per-root search state
-  int64_t words = 0;
-  uint32_t *bitmaps = nullptr;  // vis | fr0 | fr1 | fr2, 4 * words
-  uint32_t *dead = nullptr;     // 1 bit per vertex: no in-edges (dead_prepare)
+  int64_t words = 0;            // ceil(n / 32)
+  uint32_t *bitmaps = nullptr;  // vis | fr0 | fr1 | fr2, 4 * bitmap_stride(n)
+  uint32_t *dead = nullptr;     // 1 bit per vertex: no in-edges (dead_prepare),
+                                // bitmap_stride(n) words
+  int64_t live = 0;             // vertices with in-edges
   int32_t *queue = nullptr;     // 2 * n
   uint32_t *bigoff = nullptr;   // 2 * bcap
   int64_t bcap = 0;

@@ -29,7 +29,7 @@ int64_t bfs_big_capacity(int64_t n, int64_t nnz);
 
 constexpr int64_t kNoAllocMaxVertices = CG_NOALLOC_MAX_VERTICES;
 constexpr int64_t kNoAllocMaxBig = CG_NOALLOC_MAX_BIG;
-constexpr int64_t kNoAllocWords = (kNoAllocMaxVertices + 31) / 32;
+constexpr int64_t kNoAllocWords = bitmap_stride(kNoAllocMaxVertices);
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffCtl = 0;
@@ -119,20 +119,23 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   p.n = n;
   p.nnz = nnz;
   p.words = words;
+  const int64_t stride = bitmap_stride(n);  // <= kNoAllocWords
+  p.tiles = stride / kTileWords;
   p.in_off = d_in_off;
   p.in_idx = d_in_idx;
   p.out_off = d_out_off ? d_out_off : d_in_off;
   p.out_idx = d_out_idx ? d_out_idx : d_in_idx;
   uint32_t *bitmaps = reinterpret_cast<uint32_t *>(base + kOffBitmaps);
   p.vis = bitmaps;
-  p.fr0 = bitmaps + words;
-  p.fr1 = bitmaps + 2 * words;
-  p.fr2 = bitmaps + 3 * words;
+  p.fr0 = bitmaps + stride;
+  p.fr1 = bitmaps + 2 * stride;
+  p.fr2 = bitmaps + 3 * stride;
   // No per-graph state is kept here, so the map of vertices without in-edges
   // that the handle API builds once is absent: pull rounds load the in-list
   // offsets of those vertices too (about 10 us more per late pull round at
   // R-MAT scale 21 than cg_bfs; results are the same).
   p.dead = nullptr;
+  p.live = n;
   int32_t *queue = reinterpret_cast<int32_t *>(base + kOffQueue);
   p.queue0 = queue;
   p.queue1 = queue + n;

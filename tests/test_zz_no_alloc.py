@@ -47,7 +47,7 @@ def _noalloc(lib, torch, a, d_in, d_out, root, stats="pageable"):
   elif stats == "pinned":
     pin = PinnedBuffer(ctypes.sizeof(_lib.CgStats), dtype=np.uint8)
     st = _lib.CgStats.from_address(pin.array.ctypes.data)
-    st_arg = ctypes.c_void_p(pin.array.ctypes.data)
+    st_arg = ctypes.pointer(st)
   else:
     st, st_arg = None, None
   rc = lib.cg_bfs_noalloc(n, a.nnz, _ptr(d_in[0]), _ptr(d_in[1]), _ptr(d_out[0]), _ptr(d_out[1]),
