@@ -321,19 +321,25 @@ int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int3
   for (int32_t i = 0; i < k; ++i)
     if (roots[i] < 0 || roots[i] >= g->n) return CG_ERR_INVALID_ARG;
   const int64_t elems = (int64_t)k * g->n;
-  int rc = msbfs_prepare(g, g->opt.lane_words, elems);
+  // Both outputs page-locked (and the lowest-index rule, whose passes write
+  // each output once): the batch's passes store straight into host memory, so
+  // the transfer runs with the output pass instead of after it.  Otherwise
+  // the batch lands in device buffers and is copied afterwards.
+  const bool fifo = g->opt.parent_rule == CG_PARENT_FIFO;
+  int32_t *hl = fifo ? nullptr : pinned_device_ptr(levels);
+  int32_t *hp = fifo ? nullptr : pinned_device_ptr(parents);
+  const bool to_host = hl && hp;
+  int rc = msbfs_prepare(g, g->opt.lane_words, to_host ? 0 : elems);
   if (rc) return rc;
   CG_CUDA(cudaEventRecord(g->ev0, g->stream));
-  rc = msbfs_launch(g, roots, k, g->ms_levels, g->ms_parents);
+  rc = msbfs_launch(g, roots, k, to_host ? hl : g->ms_levels, to_host ? hp : g->ms_parents);
   if (rc) return rc;
-  if (g->opt.parent_rule == CG_PARENT_FIFO &&
-      (rc = fifo_all(g, roots, k, g->ms_levels, g->ms_parents)))
-    return rc;
+  if (fifo && (rc = fifo_all(g, roots, k, g->ms_levels, g->ms_parents))) return rc;
   CG_CUDA(cudaEventRecord(g->ev1, g->stream));
   const size_t bytes = sizeof(int32_t) * (size_t)elems;
-  if (levels)
+  if (levels && !to_host)
     CG_CUDA(cudaMemcpyAsync(levels, g->ms_levels, bytes, cudaMemcpyDeviceToHost, g->stream));
-  if (parents)
+  if (parents && !to_host)
     CG_CUDA(cudaMemcpyAsync(parents, g->ms_parents, bytes, cudaMemcpyDeviceToHost, g->stream));
   cg_stats local;
   CG_CUDA(cudaMemcpyAsync(&local, g->d_stats, sizeof(cg_stats), cudaMemcpyDeviceToHost, g->stream));

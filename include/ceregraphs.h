@@ -162,7 +162,10 @@ int cg_graph_last_stats(cg_graph *g, cg_stats *stats);
  * pass, cg_options.lane_words), a boolean SpMM per round.  No reference
  * counterpart as one call: it replaces run_graph500.py:321-440's per-root
  * loop of seed/launch/readback.  Outputs are root-major: levels[i * n + v].
- * Host buffers of k * n int32 each (either may be NULL); blocks. */
+ * Host buffers of k * n int32 each (either may be NULL); blocks.  When both are
+ * page-locked (cg_host_alloc) and the parent rule is CG_PARENT_LOWEST, the
+ * batch's kernels store the outputs straight into them (the transfer runs
+ * during the output pass); otherwise they are copied after the batch. */
 int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int32_t *parents,
              cg_stats *stats);
 /* Device-pointer form (both outputs required), enqueued on the handle's

@@ -212,3 +212,25 @@ def test_msbfs_more_parents_than_records(built_lib, oracle_mod, lane_words, dire
     lv, pa, st = g.msbfs(roots[:k])
     assert st["status"] == 0
     assert np.array_equal(lv, rl) and np.array_equal(pa, rp)
+
+
+@pytest.mark.parametrize("graph", ["rmat16", "grid96"])
+def test_msbfs_into_page_locked_host_buffers(built_lib, oracle_mod, graph):
+  """Page-locked outputs: the batch's kernels write host memory directly (two
+  passes of 64 lanes; the 96 x 96 grid is deeper than the round history, so its
+  batch runs in the direct kernel).  Equal to the oracle bit for bit."""
+  from ceregraphs_gb300.engine import PinnedBuffer
+  a = generators.rmat(16, 16, 0) if graph == "rmat16" else generators.grid2d(96)
+  roots = graph500.pick_sources(a, 80, 2)
+  k = len(roots)
+  rl, rp, rounds = _oracle_all(oracle_mod, a, roots)
+  with Graph(a) as g:
+    lv, pa = PinnedBuffer((k, a.n)), PinnedBuffer((k, a.n))
+    lv.array[:] = 7
+    pa.array[:] = 7
+    _, _, st = g.msbfs(roots, lv.array, pa.array)
+    assert st["status"] == 0
+    assert np.array_equal(lv.array, rl)
+    assert np.array_equal(pa.array, rp)
+    lv.free()
+    pa.free()
