@@ -100,6 +100,7 @@ class ServeReport:
   queries: list = field(default_factory=list)
   wall_s: float = 0.0
   steps: int = 0
+  unserved: int = 0   # arrivals not started when the run's time limit ran out
 
   def latencies_ms(self):
     return np.array([(q.t_done - q.t_arrival) * 1e3 for q in self.queries])
@@ -107,7 +108,7 @@ class ServeReport:
   def summary(self):
     lat = self.latencies_ms()
     n = len(lat)
-    return {"queries": n, "wall_s": self.wall_s,
+    return {"queries": n, "unserved": self.unserved, "wall_s": self.wall_s,
             "throughput_qps": n / self.wall_s if self.wall_s > 0 else float("nan"),
             "p50_ms": float(np.percentile(lat, 50)) if n else float("nan"),
             "p99_ms": float(np.percentile(lat, 99)) if n else float("nan"),
@@ -168,9 +169,11 @@ class Server:
   def _bytes(self, name):
     return 8 * self.graphs[name].n
 
-  def run(self, arrivals, realtime=True):
+  def run(self, arrivals, realtime=True, time_limit=None):
     """Serve [(t, graph, root)].  With realtime the host clock paces the
-    arrivals; otherwise every query is available at once (throughput mode)."""
+    arrivals; otherwise every query is available at once (throughput mode).
+    After `time_limit` seconds no query is admitted any more: those in flight
+    finish, the rest count as unserved."""
     torch = self.torch
     torch.cuda.synchronize()
     waiting = {k: deque() for k in self.graphs}
@@ -180,6 +183,13 @@ class Server:
     t0 = time.perf_counter()
     clock = (lambda: time.perf_counter() - t0) if realtime else (lambda: float("inf"))
     while todo or any(waiting[k] or inflight[k] for k in self.graphs):
+      if time_limit is not None and time.perf_counter() - t0 > time_limit:
+        report.unserved += len(todo) + sum(len(w) for w in waiting.values())
+        todo.clear()
+        for w in waiting.values():
+          w.clear()
+        if not any(inflight.values()):
+          break
       now = clock()
       while todo and todo[0].t_arrival <= now:
         q = todo.popleft()
@@ -286,7 +296,8 @@ class BatchServer:
       q.levels, q.parents = lv[i], pa[i]
     return done
 
-  def run(self, arrivals, realtime=True):
+  def run(self, arrivals, realtime=True, time_limit=None):
+    """As Server.run: after `time_limit` seconds nothing new is launched."""
     torch = self.torch
     torch.cuda.synchronize()
     waiting = {k: deque() for k in self.graphs}
@@ -296,6 +307,13 @@ class BatchServer:
     t0 = time.perf_counter()
     clock = (lambda: time.perf_counter() - t0) if realtime else (lambda: float("inf"))
     while todo or inflight or any(waiting.values()):
+      if time_limit is not None and time.perf_counter() - t0 > time_limit:
+        report.unserved += len(todo) + sum(len(w) for w in waiting.values())
+        todo.clear()
+        for w in waiting.values():
+          w.clear()
+        if not inflight:
+          break
       now = clock()
       while todo and todo[0].t_arrival <= now:
         q = todo.popleft()
@@ -344,9 +362,10 @@ class BatchServer:
     pass
 
 
-def serial_baseline(graphs, arrivals, realtime=True, on_done=None):
+def serial_baseline(graphs, arrivals, realtime=True, on_done=None, time_limit=None):
   """The same arrivals served one query at a time (FIFO) through cg_bfs with
-  device outputs (no batching)."""
+  device outputs (no batching); after `time_limit` seconds the rest are
+  unserved."""
   import torch
   bufs = {k: (torch.empty(g.n, dtype=torch.int32, device="cuda"),
               torch.empty(g.n, dtype=torch.int32, device="cuda")) for k, g in graphs.items()}
@@ -355,6 +374,9 @@ def serial_baseline(graphs, arrivals, realtime=True, on_done=None):
   t0 = time.perf_counter()
   for i, (t, name, root) in enumerate(arrivals):
     now = time.perf_counter() - t0
+    if time_limit is not None and now > time_limit:
+      report.unserved = len(arrivals) - i
+      break
     if realtime and t > now:
       time.sleep(t - now)
     q = Query(i, name, root, t if realtime else time.perf_counter() - t0)

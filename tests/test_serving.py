@@ -201,3 +201,27 @@ def test_budget_below_one_query_is_refused():
     serving.BatchServer(graphs, hbm_budget_bytes=100)
   with pytest.raises(ValueError):
     serving.Server(graphs, hbm_budget_bytes=100)
+
+
+@pytest.mark.gpu
+def test_time_limit_stops_admission_and_counts_the_rest(built_lib):
+  """Every mode stops taking queries once its time limit has passed: the
+  queries it served plus those it reports unserved are all the arrivals, and
+  those it served are complete."""
+  from ceregraphs_gb300.engine import Graph
+  a = generators.rmat(14, 16, 3)
+  graphs = {"rmat14": Graph(a)}
+  roots = {"rmat14": graph500.pick_sources(a, 200, 5)}
+  arrivals = serving.poisson_arrivals(20000.0, 2000, roots, seed=6)
+  runs = [serving.BatchServer(graphs, batch_min=4).run(arrivals, time_limit=0.02),
+          serving.serial_baseline(graphs, arrivals, time_limit=0.02)]
+  srv = serving.Server(graphs)
+  runs.append(srv.run(arrivals, time_limit=0.02))
+  srv.close()
+  for rep in runs:
+    s = rep.summary()
+    assert s["queries"] + s["unserved"] == len(arrivals)
+    assert s["unserved"] > 0
+    assert all(q.t_done >= q.t_arrival for q in rep.queries)
+  for g in graphs.values():
+    g.close()
