@@ -39,6 +39,8 @@ CG_PARENT_FIFO = 1    # scipy breadth_first_order's predecessor (run_graph500.py
 CG_GRAPH_DEVICE_PTRS = 1
 CG_GRAPH_SYMMETRIC = 2
 
+CG_ORDER_DEGREE = 1  # cg_graph_reorder: descending in-degree (util/analyze.cpp:226-372)
+
 CG_HISTORY = 64
 
 
@@ -134,6 +136,7 @@ SIGNATURES = {
     "cg_graph_from_edges": ([ctypes.c_int64, ctypes.c_int64, _P, _P, ctypes.c_int32,
                              ctypes.POINTER(_P)], ctypes.c_int),
     "cg_graph_export": ([_P, _P, _P, _P, _P], ctypes.c_int),
+    "cg_graph_reorder": ([_P, ctypes.c_int32, ctypes.POINTER(_P)], ctypes.c_int),
     "cg_parse_edges": ([ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32,
                         ctypes.POINTER(CgEdgeList)], ctypes.c_int),
     "cg_edge_list_free": ([ctypes.POINTER(CgEdgeList)], ctypes.c_int),

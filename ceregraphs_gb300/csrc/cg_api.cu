@@ -44,6 +44,8 @@ static void free_graph(cg_graph *g) {
   cudaFree(g->d_stats);
   cudaFree(g->tmp_levels);
   cudaFree(g->tmp_parents);
+  cudaFree(g->orig);
+  cudaFree(g->perm);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
   if (g->h_stats) cudaFreeHost(g->h_stats);
@@ -218,6 +220,10 @@ void *cg_graph_stream(const cg_graph *g) { return g ? (void *)g->stream : nullpt
 
 int cg_bfs_device(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents) {
   if (!g || !d_levels || !d_parents || root < 0 || root >= g->n) return CG_ERR_INVALID_ARG;
+  if (g->opt.parent_rule == CG_PARENT_FIFO) {
+    const int r = refuse_reordered(g, "the FIFO parent rule");
+    if (r) return r;
+  }
   const int rc = bfs_launch(g, root, d_levels, d_parents);
   if (rc || g->opt.parent_rule != CG_PARENT_FIFO) return rc;
   return fifo_parents(g, root, d_levels, d_parents);
@@ -245,6 +251,10 @@ static int32_t *pinned_device_ptr(int32_t *host) {
 
 int cg_bfs(cg_graph *g, int64_t root, int32_t *levels, int32_t *parents, cg_stats *stats) {
   if (!g || root < 0 || root >= g->n) return CG_ERR_INVALID_ARG;
+  if (g->opt.parent_rule == CG_PARENT_FIFO) {
+    const int r = refuse_reordered(g, "the FIFO parent rule");
+    if (r) return r;
+  }
   if (!g->tmp_levels) {
     if (cudaMalloc(&g->tmp_levels, sizeof(int32_t) * (size_t)g->n) != cudaSuccess)
       return CG_ERR_OUT_OF_MEMORY;
@@ -308,6 +318,7 @@ static int fifo_all(cg_graph *g, const int64_t *roots, int32_t k, const int32_t 
 int cg_msbfs_device(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_levels,
                     int32_t *d_parents) {
   if (!g || !roots || k <= 0 || !d_levels || !d_parents) return CG_ERR_INVALID_ARG;
+  if (int r = refuse_reordered(g, "cg_msbfs_device")) return r;
   for (int32_t i = 0; i < k; ++i)
     if (roots[i] < 0 || roots[i] >= g->n) return CG_ERR_INVALID_ARG;
   int rc = msbfs_launch(g, roots, k, d_levels, d_parents);
@@ -318,6 +329,7 @@ int cg_msbfs_device(cg_graph *g, const int64_t *roots, int32_t k, int32_t *d_lev
 int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int32_t *parents,
              cg_stats *stats) {
   if (!g || !roots || k <= 0) return CG_ERR_INVALID_ARG;
+  if (int r = refuse_reordered(g, "cg_msbfs")) return r;
   for (int32_t i = 0; i < k; ++i)
     if (roots[i] < 0 || roots[i] >= g->n) return CG_ERR_INVALID_ARG;
   const int64_t elems = (int64_t)k * g->n;
@@ -353,6 +365,7 @@ int cg_msbfs(cg_graph *g, const int64_t *roots, int32_t k, int32_t *levels, int3
 
 int cg_count_edges(cg_graph *g, const int32_t *d_levels, int32_t k, int64_t *m_out) {
   if (!g || !d_levels || k <= 0 || k > 65535 || !m_out) return CG_ERR_INVALID_ARG;
+  if (int r = refuse_reordered(g, "cg_count_edges")) return r;
   unsigned long long *d_m = nullptr;
   if (cudaMallocAsync((void **)&d_m, sizeof(unsigned long long) * (size_t)k, g->stream) !=
       cudaSuccess)

@@ -83,6 +83,12 @@ __device__ __forceinline__ uint4 ldg4(const uint32_t *a) {
 __device__ __forceinline__ void st4(uint32_t *a, uint4 v) { *reinterpret_cast<uint4 *>(a) = v; }
 __device__ __forceinline__ bool any4(uint4 v) { return (v.x | v.y | v.z | v.w) != 0u; }
 
+// Original id of resident vertex v (the identity unless the graph was
+// relabelled): the output position and the parent value outputs use.
+__device__ __forceinline__ int32_t orig_id(const BfsParams &p, int64_t v) {
+  return p.orig ? __ldg(p.orig + v) : (int32_t)v;
+}
+
 // Bits of word `wi` that stand for vertices < n.
 __device__ __forceinline__ uint32_t valid_bits(int64_t wi, int64_t n) {
   const int64_t lo = wi * 32;
@@ -182,11 +188,12 @@ __device__ __forceinline__ bool relax_push(const BfsParams &p, const uint32_t *c
                                            uint32_t *nxt, int32_t u, int32_t v, int next_level) {
   const uint32_t w = (uint32_t)v >> 5, bit = 1u << (v & 31);
   if ((p.vis[w] | cur[w]) & bit) return false;
-  atomicMin(reinterpret_cast<unsigned *>(p.parents) + v, (unsigned)u);
+  const int32_t ov = orig_id(p, v);
+  atomicMin(reinterpret_cast<unsigned *>(p.parents) + ov, (unsigned)orig_id(p, u));
   if (nxt[w] & bit) return false;
   const unsigned old = atomicOr(nxt + w, bit);
   if (old & bit) return false;
-  p.levels[v] = next_level;
+  p.levels[ov] = next_level;
   return true;
 }
 
@@ -464,9 +471,9 @@ __device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nx
 #pragma unroll
           for (int q = 1; q < kPullThreadScan; ++q)
             if (q == k) uk = u[q];
-          const int64_t v = v0 + j * 32 + bit;
-          p.parents[v] = uk;
-          p.levels[v] = L + 1;
+          const int32_t ov = orig_id(p, v0 + j * 32 + bit);
+          p.parents[ov] = orig_id(p, uk);
+          p.levels[ov] = L + 1;
           found = true;
         }
         pos += kPullThreadScan;
@@ -493,8 +500,9 @@ __device__ void pull_round(const BfsParams &p, const uint32_t *cur, uint32_t *nx
           const unsigned who = __ballot_sync(kFull, hit);
           if (who) {
             if (lane == __ffs(who) - 1) {
-              p.parents[vj] = u;
-              p.levels[vj] = L + 1;
+              const int32_t ovj = orig_id(p, vj);
+              p.parents[ovj] = orig_id(p, u);
+              p.levels[ovj] = L + 1;
             }
             got = true;
             break;
@@ -722,15 +730,17 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
   BfsCtl *ctl = p.ctl;
   const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  const int32_t root = (int32_t)p.root;
+  // the root in original ids (output positions) and as a resident vertex
+  const int32_t root_out = (int32_t)p.root;
+  const int32_t root = p.perm ? __ldg(p.perm + p.root) : root_out;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 
   // ---- phase 0: start_spmv -- reset outputs and bitmaps, seed the root ----
   __shared__ SearchState ss;  // thread 0's copy of the search-wide bookkeeping
   if (leader) ss.t_mark = global_ns();
   for (int64_t i = gtid; i < p.n; i += nthreads) {
-    p.levels[i] = (i == root) ? 0 : -1;
-    p.parents[i] = (i == root) ? root : -1;
+    p.levels[i] = (i == root_out) ? 0 : -1;
+    p.parents[i] = (i == root_out) ? root_out : -1;
   }
   // whole tiles (the padding past `words` too: a bitmap-wide round reads it)
   const uint4 zero4 = make_uint4(0u, 0u, 0u, 0u);
@@ -1080,6 +1090,8 @@ int bfs_launch(cg_graph *g, int64_t root, int32_t *d_levels, int32_t *d_parents,
   p.fr2 = g->bitmaps + 3 * stride;
   p.dead = g->dead;
   p.live = g->live;
+  p.orig = g->orig;
+  p.perm = g->perm;
   p.queue0 = g->queue;
   p.queue1 = g->queue + g->n;
   p.bigoff0 = g->bigoff;

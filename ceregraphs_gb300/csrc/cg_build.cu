@@ -380,6 +380,9 @@ int cg_graph_from_edges(int64_t n, int64_t m, const uint32_t *d_src, const uint3
 
 int cg_graph_export(const cg_graph *g, int64_t *in_off, int32_t *in_idx, int64_t *out_off,
                     int32_t *out_idx) {
+  if (g) {
+    if (int r = refuse_reordered(g, "cg_graph_export")) return r;
+  }
   if (!g) return CG_ERR_INVALID_ARG;
   const size_t ob = sizeof(int64_t) * (size_t)(g->n + 1), ib = sizeof(int32_t) * (size_t)g->nnz;
   if (in_off) CG_CUDA(cudaMemcpyAsync(in_off, g->in_off, ob, cudaMemcpyDeviceToHost, g->stream));

@@ -96,6 +96,10 @@ struct BfsParams {
   const uint32_t *dead;  // vertices without in-edges (never reached), or null; bits
                          // past n are set, `stride` words
   int64_t live;          // vertices with in-edges (n when `dead` is null)
+  // Relabelled graph (cg_graph_reorder), or null: orig[v] is the original id
+  // of resident vertex v and perm its inverse.  Roots come in original ids;
+  // outputs are written at original positions with original parent ids.
+  const int32_t *orig, *perm;
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   int32_t *levels, *parents;
@@ -136,6 +140,11 @@ struct cg_graph {
   uint32_t *dead = nullptr;     // 1 bit per vertex: no in-edges (dead_prepare),
                                 // bitmap_stride(n) words
   int64_t live = 0;             // vertices with in-edges
+  // cg_graph_reorder: resident vertex v is original vertex orig[v]; perm is
+  // the inverse (both int32[n], null for a graph in its original order)
+  int32_t *orig = nullptr;
+  int32_t *perm = nullptr;
+  int32_t reorder = 0;          // CG_ORDER_* the handle was built with
   int32_t *queue = nullptr;     // 2 * n
   uint32_t *bigoff = nullptr;   // 2 * bcap
   int64_t bcap = 0;
@@ -169,6 +178,9 @@ int dead_prepare(cg_graph *g);
 // captured: for set-up that has to synchronise the handle's stream.
 int refuse_setup_in_capture(cg_graph *g);
 int msbfs_prepare(cg_graph *g, int lane_words, int64_t out_elems);
+// CG_ERR_NOT_SUPPORTED (with a reason naming `what`) on a graph made by
+// cg_graph_reorder, whose relabelled arrays only the per-root search maps back.
+int refuse_reordered(const cg_graph *g, const char *what);
 void msbfs_release(cg_graph *g);
 // Rewrites the parents of a finished search (d_levels final) by the FIFO rule
 // of scipy's breadth_first_order; synchronises with the handle's stream.

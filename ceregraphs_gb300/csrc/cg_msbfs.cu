@@ -1134,6 +1134,9 @@ using namespace cg;
 extern "C" {
 
 int cg_pool_create(cg_graph *g, int32_t lane_words, cg_pool **out) {
+  if (g) {
+    if (int r = refuse_reordered(g, "cg_pool_create")) return r;
+  }
   if (!g || !out || (lane_words != 1 && lane_words != 2)) return CG_ERR_INVALID_ARG;
   *out = nullptr;
   cg_pool *pl = new (std::nothrow) cg_pool();

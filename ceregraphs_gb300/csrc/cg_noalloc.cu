@@ -136,6 +136,7 @@ extern "C" int cg_bfs_noalloc(int64_t n, int64_t nnz, const int64_t *d_in_off,
   // R-MAT scale 21 than cg_bfs; results are the same).
   p.dead = nullptr;
   p.live = n;
+  p.orig = p.perm = nullptr;
   int32_t *queue = reinterpret_cast<int32_t *>(base + kOffQueue);
   p.queue0 = queue;
   p.queue1 = queue + n;

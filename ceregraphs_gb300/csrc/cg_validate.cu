@@ -188,6 +188,9 @@ using namespace cg;
 extern "C" int cg_validate_device(cg_graph *g, const int64_t *roots, int32_t k,
                                   const int32_t *d_levels, const int32_t *d_parents,
                                   cg_validation *out) {
+  if (g) {
+    if (int r = refuse_reordered(g, "cg_validate_device")) return r;
+  }
   if (!g || !roots || k <= 0 || k > 65535 || !d_levels || !d_parents || !out)
     return CG_ERR_INVALID_ARG;
   for (int32_t i = 0; i < k; ++i)

@@ -125,6 +125,13 @@ class Graph:
           "cg_graph_export")
     return GraphArrays(self.n, self.nnz, io, ii, oo, oi, self.symmetric)
 
+  def reorder(self, order=_lib.CG_ORDER_DEGREE):
+    """A degree-ordered resident copy for per-root searches (cg_graph_reorder):
+    same roots, same outputs in original ids, vertices laid out hubs first."""
+    h = ctypes.c_void_p()
+    check(_lib.load().cg_graph_reorder(self._h, int(order), ctypes.byref(h)), "cg_graph_reorder")
+    return Graph.from_handle(h)
+
   def export_offsets(self):
     """The resident CSR offsets (n + 1 int64) on the host."""
     io = np.empty(self.n + 1, dtype=np.int64)

@@ -306,6 +306,24 @@ typedef struct cg_validation {
 int cg_validate_device(cg_graph *g, const int64_t *roots, int32_t k, const int32_t *d_levels,
                        const int32_t *d_parents, cg_validation *out);
 
+/* ---- degree-aware reordering ----------------------------------------------
+ * The one-GPU counterpart of the reference's vertex balancing
+ * (util/analyze.cpp:226-372), keeping vertex identity as its --operm option
+ * does (util/analyze.cpp:431-437).  cg_graph_reorder builds a second resident
+ * handle whose vertices are numbered by descending in-degree (ties by id) --
+ * hubs first, vertices without in-edges last -- for locality of the frontier
+ * bits and list offsets a search touches.  Each in-list keeps ascending
+ * ORIGINAL id order.  Per-root searches on it (cg_bfs, cg_bfs_device and
+ * captures of them) take roots in original ids and return levels and parents
+ * at original positions with original parent ids, bit-identical to the
+ * original handle's (lowest-index rule).  Everything else is refused with
+ * CG_ERR_NOT_SUPPORTED on the reordered handle: batched searches, pools, the
+ * FIFO parent rule, cg_count_edges, cg_validate_device, cg_graph_export --
+ * run those on the original handle.  The original handle stays valid; each
+ * is destroyed separately. */
+enum { CG_ORDER_DEGREE = 1 };
+int cg_graph_reorder(const cg_graph *g, int32_t order, cg_graph **out);
+
 /* ---- one search without any library allocation --------------------------
  * No counterpart in the reference.  For callers that cannot let this library
  * allocate device memory: runtimes that reserve and budget the GPU's memory
