@@ -39,7 +39,7 @@ METRIC = "per-root BFS GTEPS, harmonic mean over the Graph500 roots"
 # DRAM bytes (read + write) per launch of bfs_persistent measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum, mean over the timed step's
 # launches) for (scale, edgefactor, seed, root seed); roofline.traffic.
-NCU_TRAFFIC_BYTES = {(21, 16, 0, 1): 84.0e6, (23, 16, 2, 3): 541.0e6}
+NCU_TRAFFIC_BYTES = {(21, 16, 0, 1): 80.5e6, (23, 16, 2, 3): 541.0e6}
 FALLBACK_HBM_GBS = 6800.0
 
 
