@@ -17,6 +17,7 @@
 
 #include <vector>
 
+#include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
 
 #include "cg_internal.cuh"
@@ -26,6 +27,10 @@ namespace cg {
 struct FifoState {
   int64_t n = 0;
   int32_t *rank = nullptr;              // [n] queue rank within the vertex's level
+  // [n] (level << 32) | rank and (level << 32) | FIFO parent of the vertices
+  // ranked so far in this pass (-1 elsewhere): one load tells a list entry's
+  // level and rank, or whether an out-neighbour is a given parent's child
+  unsigned long long *lr = nullptr, *pl = nullptr;
   int32_t *order = nullptr;             // [n] vertices of levels >= 1, grouped by level
   unsigned long long *keys = nullptr;   // [n] (parent rank, vertex) of one level
   unsigned long long *sorted = nullptr; // [n]
@@ -124,11 +129,204 @@ __global__ void fifo_pick_kernel(const int64_t *__restrict__ in_off,
 }
 
 __global__ void fifo_rank_kernel(const unsigned long long *__restrict__ sorted, unsigned count,
-                                 int vbits, int32_t *rank) {
+                                 int vbits, int level, int32_t *rank, unsigned long long *lr) {
   const unsigned long long vmask = (1ull << vbits) - 1ull;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-       i += (int64_t)gridDim.x * blockDim.x)
-    rank[sorted[i] & vmask] = (int32_t)i;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long v = sorted[i] & vmask;
+    rank[v] = (int32_t)i;
+    lr[v] = ((unsigned long long)level << 32) | (unsigned long long)i;
+  }
+}
+
+// Levels of at most kSmallLevel vertices are handled by one block, many
+// levels to a launch, with no sort: level L+1's queue is level L's queue in
+// order with each vertex's children (the out-neighbours whose FIFO parent it
+// is) appended in out-list order, which is ascending -- the same order the
+// sort of (parent rank, id) gives.  Per level: (1) every child picks its
+// parent, the level-L in-neighbour of smallest rank (one 8-byte load of
+// (level, rank) per in-list entry), records (level + 1, parent) for the
+// parent's scan and counts itself in its parent's shared-memory counter;
+// (2) a block scan of the counts in rank order gives each parent its first
+// child's rank; (3) every parent with children walks its out-list handing
+// out ranks to the entries recorded as its children.  Long lists go to a
+// warp.  One SM's load pipeline bounds this, so each list entry costs one
+// load.  On deep graphs launches would otherwise dominate (a 4096 x 4096 grid
+// has ~8000 levels).
+constexpr int kSmallThreads = 1024;
+constexpr int kSmallPer = 8;                                // counts a thread scans
+constexpr int kSmallLevel = kSmallThreads * kSmallPer;     // vertices per level, at most
+constexpr int kHeavyList = 64;  // list length above which a warp scans
+using SmallScan = cub::BlockScan<unsigned, kSmallThreads>;
+struct SmallSmem {
+  int32_t queue[2][kSmallLevel];     // levels L and L+1 in queue (rank) order
+  unsigned cnt[kSmallLevel + 1];     // children per parent rank, then first ranks
+  int32_t heavy[kSmallLevel];        // positions whose lists a warp scans
+  unsigned nheavy;
+  typename SmallScan::TempStorage scan;
+};
+
+__device__ __forceinline__ unsigned long long warp_min64(unsigned long long x) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, x, d);
+    x = o < x ? o : x;
+  }
+  return x;
+}
+
+// Over in-list entries [s, e) (lanes lane, lane + step, ...), the smallest
+// (rank << 32) | u of a level-L in-neighbour u; lr is written by this block at
+// earlier levels, so it is read with ordinary loads, never the read-only path.
+__device__ __forceinline__ unsigned long long fifo_best(const int32_t *__restrict__ in_idx,
+                                                        const unsigned long long *lr, int64_t s,
+                                                        int64_t e, int L, int lane, int step) {
+  unsigned long long best = ~0ull;
+  for (int64_t j = s + lane; j < e; j += step) {
+    const int32_t u = __ldg(in_idx + j);
+    const unsigned long long x = lr[u];
+    if ((unsigned)(x >> 32) == (unsigned)L) {
+      const unsigned long long k = ((x & 0xffffffffull) << 32) | (uint32_t)u;
+      best = k < best ? k : best;
+    }
+  }
+  return best;
+}
+
+// Level L+1 vertex w takes parent u (rank r among level L).
+__device__ __forceinline__ void fifo_adopt(int32_t w, unsigned long long best, int L,
+                                           int32_t *parents, unsigned long long *pl,
+                                           unsigned *cnt) {
+  if (best == ~0ull) return;  // no level-L in-neighbour: not a level-(L+1) vertex
+  const int32_t u = (int32_t)(uint32_t)best;
+  parents[w] = u;
+  pl[w] = ((unsigned long long)(L + 1) << 32) | (uint32_t)u;
+  atomicAdd(&cnt[best >> 32], 1u);
+}
+
+// One block: levels L0 .. L1-1 in turn; for each, level L has counts[L] and
+// level L+1 counts[L+1] vertices, both at most kSmallLevel; order[offs[L+1] ..]
+// lists level L+1 in no particular order.
+__global__ void __launch_bounds__(kSmallThreads) fifo_small_levels_kernel(
+    const int64_t *__restrict__ in_off, const int32_t *__restrict__ in_idx,
+    const int64_t *__restrict__ out_off, const int32_t *__restrict__ out_idx, int32_t *rank,
+    unsigned long long *lr, unsigned long long *pl, const int32_t *__restrict__ order,
+    const unsigned *__restrict__ counts, const unsigned *__restrict__ offs, int L0, int L1,
+    int32_t root, int32_t *parents) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  SmallSmem &S = *reinterpret_cast<SmallSmem *>(s_raw);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  constexpr int kWarps = kSmallThreads / 32;
+  int cur = 0;
+  // level L0 in queue order, from the ranks already assigned (level 0 is the
+  // root alone; order[] lists levels >= 1)
+  if (L0 == 0) {
+    if (t == 0) S.queue[0][0] = root;
+  } else {
+    for (unsigned i = t; i < counts[L0]; i += kSmallThreads) {
+      const int32_t u = order[offs[L0] + i];
+      S.queue[0][rank[u]] = u;
+    }
+  }
+  for (int L = L0; L < L1; ++L) {
+    const unsigned c = counts[L + 1], p = counts[L];
+    const unsigned base = offs[L + 1];
+    int32_t *qL = S.queue[cur];
+    int32_t *qN = S.queue[cur ^ 1];
+    for (unsigned r = t; r < p; r += kSmallThreads) S.cnt[r] = 0;
+    if (t == 0) S.nheavy = 0;
+    __syncthreads();
+    // (1) parents of level L+1
+    for (unsigned pos = t; pos < c; pos += kSmallThreads) {
+      const int32_t w = order[base + pos];
+      const int64_t s = __ldg(in_off + w), e = __ldg(in_off + w + 1);
+      if (e - s > kHeavyList)
+        S.heavy[atomicAdd(&S.nheavy, 1u)] = w;
+      else
+        fifo_adopt(w, fifo_best(in_idx, lr, s, e, L, 0, 1), L, parents, pl, S.cnt);
+    }
+    __syncthreads();
+    for (unsigned h = warp; h < S.nheavy; h += kWarps) {
+      const int32_t w = S.heavy[h];
+      const unsigned long long best =
+          warp_min64(fifo_best(in_idx, lr, __ldg(in_off + w), __ldg(in_off + w + 1), L, lane, 32));
+      if (lane == 0) fifo_adopt(w, best, L, parents, pl, S.cnt);
+    }
+    __syncthreads();  // every warp is done with the list before it is reset
+    // (2) first rank of each parent's children: exclusive scan in rank order
+    {
+      unsigned v[kSmallPer], sum = 0;
+#pragma unroll
+      for (int i = 0; i < kSmallPer; ++i) {
+        const unsigned r = t * kSmallPer + i;
+        v[i] = r < p ? S.cnt[r] : 0u;
+        sum += v[i];
+      }
+      unsigned before = 0;
+      SmallScan(S.scan).ExclusiveSum(sum, before);
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < kSmallPer; ++i) {
+        const unsigned r = t * kSmallPer + i;
+        if (r < p) S.cnt[r] = before;
+        before += v[i];
+      }
+      if (t == 0) {
+        S.cnt[p] = c;
+        S.nheavy = 0;
+      }
+    }
+    __syncthreads();
+    // (3) ranks of level L+1: parents with children walk their out-lists
+    const unsigned long long tag = (unsigned long long)(L + 1) << 32;
+    for (unsigned r = t; r < p; r += kSmallThreads) {
+      unsigned at = S.cnt[r];
+      const unsigned end = S.cnt[r + 1];
+      if (at == end) continue;
+      const int32_t u = qL[r];
+      const int64_t s = __ldg(out_off + u), e = __ldg(out_off + u + 1);
+      if (e - s > kHeavyList) {
+        S.heavy[atomicAdd(&S.nheavy, 1u)] = (int32_t)r;
+        continue;
+      }
+      const unsigned long long mine = tag | (uint32_t)u;
+      for (int64_t j = s; j < e && at < end; ++j) {
+        const int32_t w = __ldg(out_idx + j);
+        if (pl[w] == mine) {
+          rank[w] = (int32_t)at;
+          lr[w] = tag | at;
+          qN[at++] = w;
+        }
+      }
+    }
+    __syncthreads();
+    for (unsigned h = warp; h < S.nheavy; h += kWarps) {
+      const unsigned r = (unsigned)S.heavy[h];
+      const int32_t u = qL[r];
+      const unsigned long long mine = tag | (uint32_t)u;
+      const int64_t s = __ldg(out_off + u), e = __ldg(out_off + u + 1);
+      unsigned at = S.cnt[r];
+      for (int64_t j0 = s; j0 < e; j0 += 32) {
+        const int64_t j = j0 + lane;
+        int32_t w = 0;
+        bool child = false;
+        if (j < e) {
+          w = __ldg(out_idx + j);
+          child = pl[w] == mine;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, child);
+        if (child) {
+          const unsigned k = at + __popc(m & ((1u << lane) - 1u));
+          rank[w] = (int32_t)k;
+          lr[w] = tag | k;
+          qN[k] = w;
+        }
+        at += __popc(m);
+      }
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
 }
 
 // Bits needed for the values 0 .. x (at least 1).
@@ -154,6 +352,8 @@ int fifo_state(cg_graph *g, FifoState **out) {
   f->n = g->n;
   const size_t n = (size_t)g->n;
   bool ok = cudaMalloc(&f->rank, sizeof(int32_t) * n) == cudaSuccess &&
+            cudaMalloc(&f->lr, sizeof(unsigned long long) * n) == cudaSuccess &&
+            cudaMalloc(&f->pl, sizeof(unsigned long long) * n) == cudaSuccess &&
             cudaMalloc(&f->order, sizeof(int32_t) * n) == cudaSuccess &&
             cudaMalloc(&f->keys, sizeof(unsigned long long) * n) == cudaSuccess &&
             cudaMalloc(&f->sorted, sizeof(unsigned long long) * n) == cudaSuccess &&
@@ -161,6 +361,10 @@ int fifo_state(cg_graph *g, FifoState **out) {
             cudaMalloc(&f->cursor, sizeof(unsigned) * (n + 1)) == cudaSuccess &&
             cudaMalloc(&f->offs, sizeof(unsigned) * (n + 1)) == cudaSuccess &&
             cudaMalloc(&f->maxlevel, sizeof(int)) == cudaSuccess;
+  if (ok)
+    ok = cudaFuncSetAttribute(fifo_small_levels_kernel,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(SmallSmem)) == cudaSuccess;
   if (ok) {
     cub::DeviceRadixSort::SortKeys(nullptr, f->temp_bytes, f->keys, f->sorted, (int)n, 0, 64,
                                    g->stream);
@@ -170,7 +374,7 @@ int fifo_state(cg_graph *g, FifoState **out) {
     fifo_free(f);
     return CG_ERR_OUT_OF_MEMORY;
   }
-  g->device_bytes += (int64_t)((sizeof(int32_t) * 2 + sizeof(unsigned long long) * 2) * n +
+  g->device_bytes += (int64_t)((sizeof(int32_t) * 2 + sizeof(unsigned long long) * 4) * n +
                                sizeof(unsigned) * 3 * (n + 1) + f->temp_bytes);
   g->fifo = f;
   *out = f;
@@ -182,6 +386,8 @@ int fifo_state(cg_graph *g, FifoState **out) {
 void fifo_free(FifoState *f) {
   if (!f) return;
   cudaFree(f->rank);
+  cudaFree(f->lr);
+  cudaFree(f->pl);
   cudaFree(f->order);
   cudaFree(f->keys);
   cudaFree(f->sorted);
@@ -226,11 +432,28 @@ int fifo_parents(cg_graph *g, int64_t root, const int32_t *d_levels, int32_t *d_
   fifo_scatter_kernel<<<grid_for(n, kFifoBlock, g->num_sms), kFifoBlock, 0, st>>>(
       n, d_levels, f->offs, f->cursor, f->order);
   CG_CUDA(cudaMemsetAsync(f->rank + root, 0, sizeof(int32_t), st));
+  CG_CUDA(cudaMemsetAsync(f->lr, 0xff, sizeof(unsigned long long) * (size_t)n, st));
+  CG_CUDA(cudaMemsetAsync(f->pl, 0xff, sizeof(unsigned long long) * (size_t)n, st));
+  CG_CUDA(cudaMemsetAsync(f->lr + root, 0, sizeof(unsigned long long), st));  // level 0, rank 0
   // keys (parent rank << vbits) | v: only the bits in use are sorted
   const int vbits = bits_for((uint64_t)(n - 1));
   for (int L = 0; L < maxlevel; ++L) {
     const unsigned c = counts[(size_t)L + 1];
     if (c == 0) break;
+    if (c <= (unsigned)kSmallLevel && counts[(size_t)L] <= (unsigned)kSmallLevel) {
+      // a run of small levels: one launch of one block
+      int L1 = L + 1;
+      while (L1 < maxlevel && counts[(size_t)L1 + 1] > 0 &&
+             counts[(size_t)L1 + 1] <= (unsigned)kSmallLevel &&
+             counts[(size_t)L1] <= (unsigned)kSmallLevel)
+        ++L1;
+      fifo_small_levels_kernel<<<1, kSmallThreads, sizeof(SmallSmem), st>>>(
+          g->in_off, g->in_idx, g->out_off, g->out_idx, f->rank, f->lr, f->pl, f->order,
+          f->counts, f->offs, L, L1, (int32_t)root, d_parents);
+      CG_CUDA(cudaGetLastError());
+      L = L1 - 1;
+      continue;
+    }
     const unsigned parents_c = counts[(size_t)L];  // ranks of level L: 0 .. parents_c - 1
     const int end_bit = vbits + bits_for(parents_c ? parents_c - 1 : 0);
     fifo_pick_kernel<<<grid_for((int64_t)c * 32, kFifoBlock, g->num_sms), kFifoBlock, 0, st>>>(
@@ -239,8 +462,8 @@ int fifo_parents(cg_graph *g, int64_t root, const int32_t *d_levels, int32_t *d_
     size_t tb = f->temp_bytes;
     CG_CUDA(cub::DeviceRadixSort::SortKeys(f->temp, tb, f->keys, f->sorted, (int)c, 0,
                                            end_bit, st));
-    fifo_rank_kernel<<<grid_for(c, kFifoBlock, g->num_sms), kFifoBlock, 0, st>>>(f->sorted, c,
-                                                                                vbits, f->rank);
+    fifo_rank_kernel<<<grid_for(c, kFifoBlock, g->num_sms), kFifoBlock, 0, st>>>(
+        f->sorted, c, vbits, L + 1, f->rank, f->lr);
   }
   CG_CUDA(cudaGetLastError());
   return CG_OK;
