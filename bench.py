@@ -710,6 +710,7 @@ def run_serving(args):
     dyn["launches"] = dict(bsrv.launches)
     srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget)
     pool = srv.run(arrivals, realtime=True, time_limit=limit).summary()
+    pool["per_root_solo"] = srv.solo
     srv.close()
     base = serving.serial_baseline(graphs, arrivals, realtime=True, time_limit=limit).summary()
     rows.append({"rate_qps": rate, "arrivals": count, "window_s": args.serving_seconds,
@@ -729,7 +730,8 @@ def run_serving(args):
                                           "together (batched launch when >= 4, else "
                                           "per-root), outputs written after the rounds",
                                "pool": "continuous batching: queries join searches in "
-                                       "flight as bit lanes of a resumable launch",
+                                       "flight as bit lanes of a resumable launch; a query "
+                                       "finding its graph idle and alone runs per-root",
                                "serial": "one per-root search at a time, FIFO"}},
           "e2e": {"value": best, "unit": "queries/s", "h2d_bytes_per_step": 8,
                   "d2h_bytes_per_step": 16,

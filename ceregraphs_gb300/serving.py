@@ -143,15 +143,21 @@ def check_budget(graphs, hbm_budget_bytes):
 
 
 class Server:
-  """Continuous batching over one pool per resident graph."""
+  """Continuous batching over one pool per resident graph: queries join the
+  searches in flight as free lanes; a query that finds its graph's pool idle
+  with no other query waiting runs as a per-root search instead."""
 
   def __init__(self, graphs, lane_words=1, hbm_budget_bytes=None, max_rounds=0,
-               on_done=None):
+               on_done=None, solo_max=1):
     import torch
     check_budget(graphs, hbm_budget_bytes)
     self.torch = torch
     self.graphs = graphs                      # name -> engine.Graph
     self.lane_words = lane_words
+    # an idle pool with at most this many queries waiting runs them as per-root
+    # searches (light load: a lone query does not pay for a lane sweep)
+    self.solo_max = solo_max
+    self.solo = 0
     self.pools = {k: Pool(g, lane_words) for k, g in graphs.items()}
     self.budget = hbm_budget_bytes
     self.in_use = 0
@@ -198,6 +204,25 @@ class Server:
         waiting[q.graph].append(q)
       for name, pool in self.pools.items():
         wq = waiting[name]
+        if wq and not inflight[name] and len(wq) <= self.solo_max:
+          g = self.graphs[name]
+          while wq:
+            q = wq.popleft()
+            lv, pa = self._buffers(name)
+            q.t_admit = time.perf_counter() - t0
+            g.bfs_device(q.root, lv, pa)
+            st = g.last_stats()
+            if st["status"] != 0:
+              raise RuntimeError(f"search failed: {st}")
+            q.t_done = time.perf_counter() - t0
+            q.levels, q.parents = lv, pa
+            if self.on_done is not None:
+              self.on_done(q)
+            q.levels = q.parents = None
+            self._free[name].append((lv, pa))
+            report.queries.append(q)
+            self.solo += 1
+          continue
         while wq:
           if self.budget is not None and self.in_use + self._bytes(name) > self.budget:
             break

@@ -110,7 +110,10 @@ def test_pool_directed_and_deep(built_lib, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_server_mix_equals_alone_under_hbm_budget(built_lib):
+@pytest.mark.parametrize("solo_max", [0, 1])
+def test_server_mix_equals_alone_under_hbm_budget(built_lib, solo_max):
+  """Queries served in the pool's mix (solo_max 0: every query through lanes;
+  1: a lone query on an idle graph runs per-root) equal their searches alone."""
   import torch
   from ceregraphs_gb300.engine import Graph
   arrays = {"rmat13": generators.rmat(13, 16, 2), "rmat15": generators.rmat(15, 8, 3)}
@@ -132,7 +135,8 @@ def test_server_mix_equals_alone_under_hbm_budget(built_lib):
     checked.append(np.array_equal(lv, wl) and np.array_equal(pa, wp))
 
   budget = 40 * 8 * max(a.n for a in arrays.values())
-  srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget, on_done=on_done)
+  srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget, on_done=on_done,
+                       solo_max=solo_max)
   orig = srv._buffers
 
   def tracked(name):
