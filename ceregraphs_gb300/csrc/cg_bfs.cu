@@ -183,17 +183,24 @@ __device__ __forceinline__ void enqueue_claims(const BfsParams &p, bool claimed,
   }
 }
 
-// Edge u -> v of a push round.  Returns true for the one thread that claims v.
+// Edge u -> v of a push round.  Returns true for the one thread that claims
+// v, with v's out-degree in deg (its offsets are loaded with the claim, so the
+// claimer does not wait for them afterwards).
 __device__ __forceinline__ bool relax_push(const BfsParams &p, const uint32_t *cur,
-                                           uint32_t *nxt, int32_t u, int32_t v, int next_level) {
+                                           uint32_t *nxt, int32_t u, int32_t v, int next_level,
+                                           int64_t &deg) {
   const uint32_t w = (uint32_t)v >> 5, bit = 1u << (v & 31);
-  if ((p.vis[w] | cur[w]) & bit) return false;
+  // the three words in one round trip: a claim bit seen set stays set
+  const uint32_t seen = p.vis[w] | cur[w], claimed = nxt[w];
+  if (seen & bit) return false;
   const int32_t ov = orig_id(p, v);
   atomicMin(reinterpret_cast<unsigned *>(p.parents) + ov, (unsigned)orig_id(p, u));
-  if (nxt[w] & bit) return false;
+  if (claimed & bit) return false;
+  const int64_t o0 = __ldg(p.out_off + v), o1 = __ldg(p.out_off + v + 1);
   const unsigned old = atomicOr(nxt + w, bit);
   if (old & bit) return false;
   p.levels[ov] = next_level;
+  deg = o1 - o0;
   return true;
 }
 
@@ -205,8 +212,7 @@ __device__ __forceinline__ void push_step(const BfsParams &p, const uint32_t *cu
   int64_t deg = 0;
   if (valid) {
     v = __ldg(p.out_idx + e);
-    claimed = relax_push(p, cur, nxt, u, v, L + 1);
-    if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+    claimed = relax_push(p, cur, nxt, u, v, L + 1, deg);
   }
   enqueue_claims(p, claimed, v, deg, next_parity, Rn, acc);
 }
@@ -260,8 +266,11 @@ __device__ __forceinline__ void gather_expand(const BfsParams &p, const uint32_t
 // Expands frontier F_L from its queue (parity L & 1): edge-balanced chunks of
 // the big vertices' combined edge list, then the light vertices 32 to a warp.
 // Item i goes to warp i first; warps that finish take the rest from a counter.
+// bigw / nlight: F_L's queue sizes ((big count << 32) | big edges, light
+// count), handed over with the barrier that ended round L - 1.
 __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32_t *nxt, int L,
-                                 RoundRec *Rc, RoundRec *Rn, Acc &acc) {
+                                 RoundRec *Rc, RoundRec *Rn, unsigned long long bigw,
+                                 unsigned nlight, Acc &acc) {
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -269,10 +278,8 @@ __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32
   const int32_t *q = parity ? p.queue1 : p.queue0;
   const uint32_t *boff = parity ? p.bigoff1 : p.bigoff0;
 
-  const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
   const unsigned nbig = (unsigned)(bigw >> 32);
   const unsigned big_edges = (unsigned)(bigw & 0xffffffffu);
-  const unsigned nlight = *(volatile unsigned *)&Rc->nlight;
   // chunks of 32 .. kPushChunk edges: small frontiers still spread over the grid
   unsigned chunk = ((big_edges / (unsigned)nwarps) + 31u) & ~31u;
   chunk = chunk < 32u ? 32u : (chunk > (unsigned)kPushChunk ? (unsigned)kPushChunk : chunk);
@@ -280,6 +287,9 @@ __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32
   const unsigned nitems = nchunks + (nlight + 31u) / 32u;
   unsigned item = (unsigned)warp_id_global();
   while (item < nitems) {
+    // the next item is claimed before this one is worked, hiding the atomic
+    unsigned nextitem = 0;
+    if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
     if (item < nchunks) {
       const unsigned x0 = item * chunk;
       const unsigned x1 = min(x0 + chunk, big_edges);
@@ -324,8 +334,6 @@ __device__ void push_round_queue(const BfsParams &p, const uint32_t *cur, uint32
       gather_expand(p, cur, nxt, idx < nlight ? q[idx] : -1, L, next_parity, Rn, acc, X.u, X.s,
                     X.x);
     }
-    unsigned nextitem = 0;
-    if (lane == 0) nextitem = (unsigned)nwarps + atomicAdd(&Rc->work, 1u);
     item = __shfl_sync(kFull, nextitem, 0);
   }
 }
@@ -636,6 +644,8 @@ struct SearchState {
   unsigned long long visited, prev_nf, explored;
   int pull_rounds, switches;
   long long t_mark;  // block 0: end of the previous round on the device clock
+  unsigned long long next_big;  // the next frontier's queue sizes (record big, nlight)
+  unsigned next_light;
 };
 
 // End of round L in warp 0 of every block, after the round's barrier: the
@@ -650,16 +660,23 @@ __device__ unsigned round_decision(const BfsParams &p, int L, int dir, SearchSta
   const int lane = lane_id();
   const int g = lane >> 3, sh = lane & (kCounterShards - 1);
   static_assert(kCounterShards == 8, "three groups of eight lanes");
-  unsigned long long x = 0;
+  unsigned long long x = 0, q = 0;
   if (g == 0) x = __ldcg(&Rn->nf[sh]);
   else if (g == 1) x = __ldcg(&Rn->mf[sh]);
   else if (g == 2) x = __ldcg(&Rn->visdeg[sh]);
+  // F_{L+1}'s queue sizes, for the next push round (same round trip)
+  if (lane == 24) q = __ldcg(&Rn->big);
+  else if (lane == 25) q = __ldcg(&Rn->nlight);
+  const unsigned long long qbig = __shfl_sync(kFull, q, 24);
+  const unsigned long long qlight = __shfl_sync(kFull, q, 25);
 #pragma unroll
   for (int o = 1; o < kCounterShards; o <<= 1) x += __shfl_xor_sync(kFull, x, o);
   const unsigned long long nf = __shfl_sync(kFull, x, 0);
   const unsigned long long mf = __shfl_sync(kFull, x, 8);
   const unsigned long long vd = __shfl_sync(kFull, x, 16);
   if (lane != 0) return 0u;
+  ss.next_big = qbig;
+  ss.next_light = (unsigned)qlight;
   const bool block0 = blockIdx.x == 0;
   ss.pull_rounds += dir == kPull ? 1 : 0;
   ss.visited += nf;
@@ -786,6 +803,9 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
     ss.explored = (unsigned long long)(__ldg(p.out_off + root + 1) - __ldg(p.out_off + root));
     ss.pull_rounds = 0;
     ss.switches = 0;
+    // F_0 = {root}: queued light or big by its degree (phase 0 above)
+    ss.next_big = ss.explored > (unsigned long long)kLightMax ? ((1ull << 32) | ss.explored) : 0ull;
+    ss.next_light = ss.explored > (unsigned long long)kLightMax ? 0u : 1u;
     if (blockIdx.x == 0 && ok0) {
       const long long now = global_ns();
       p.stats->setup_ns = now - ss.t_mark;
@@ -810,18 +830,16 @@ __global__ void __launch_bounds__(kBfsBlock, 3) bfs_persistent(BfsParams p) {
     uint32_t *old = fr2;        // F_{L-1}
     if (dir == kPush) {
       if (queued)
-        push_round_queue(p, cur, nxt, L, Rc, Rn, acc);
+        push_round_queue(p, cur, nxt, L, Rc, Rn, ss.next_big, ss.next_light, acc);
       else
         push_round_bitmap(p, cur, nxt, L, Rc, Rn, heavy, acc);
       // vis |= F_L (readers test vis | F_L, so this races with nothing) and
       // clear F_{L-1}, which becomes the next round's output bitmap; a pull
       // round does both in its own tile pass
       for (int64_t i = gtid; i < p.tiles * (kTileWords / 4); i += nthreads) {
-        const uint4 c = ld4(cur + 4 * i);
-        if (any4(c)) {
-          const uint4 vv = ld4(p.vis + 4 * i);
+        const uint4 c = ld4(cur + 4 * i), vv = ld4(p.vis + 4 * i);
+        if (any4(c))
           st4(p.vis + 4 * i, make_uint4(vv.x | c.x, vv.y | c.y, vv.z | c.z, vv.w | c.w));
-        }
         st4(old + 4 * i, zero4);
       }
     } else {
