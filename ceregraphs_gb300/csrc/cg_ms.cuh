@@ -68,6 +68,11 @@ struct MsParams {
   uint32_t *touched0, *touched1, *touched2;
   uint32_t *scanmap;  // light vertices with lanes their records leave open (ledger)
   const uint32_t *dead;  // vertices without in-edges (never reached after round 0)
+  // ledger batches: vertices of in-degree 1 .. kPullLight (static), and those
+  // of them a batch has finished -- every running lane visited (no lane can
+  // reach them again), so later pull rounds skip them
+  const uint32_t *light;
+  uint32_t *fin;
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
@@ -199,12 +204,18 @@ __device__ __forceinline__ Mask<W> lane_mask(int k) {
   return m;
 }
 
+// OR over the warp: one redux.sync per 32-bit half (a shuffle tree would be
+// five dependent shuffle round trips per half).
+__device__ __forceinline__ uint64_t warp_or64(uint64_t x) {
+  const unsigned lo = __reduce_or_sync(kMsFull, (unsigned)x);
+  const unsigned hi = __reduce_or_sync(kMsFull, (unsigned)(x >> 32));
+  return ((uint64_t)hi << 32) | lo;
+}
+
 template <int W>
 __device__ __forceinline__ Mask<W> warp_or(Mask<W> m) {
 #pragma unroll
-  for (int j = 0; j < W; ++j)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m.w[j] |= __shfl_xor_sync(kMsFull, m.w[j], o);
+  for (int j = 0; j < W; ++j) m.w[j] = warp_or64(m.w[j]);
   return m;
 }
 
@@ -483,12 +494,7 @@ __device__ __forceinline__ void ms_block_totals(MsAcc &acc, MsAcc &tot) {
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const unsigned long long a = ms_warp_sum(acc.nf), b = ms_warp_sum(acc.visits),
                            c = ms_warp_sum(acc.mf);
-  unsigned long long l0 = acc.lanes[0], l1 = acc.lanes[1];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    l0 |= __shfl_xor_sync(kMsFull, l0, o);
-    l1 |= __shfl_xor_sync(kMsFull, l1, o);
-  }
+  const unsigned long long l0 = warp_or64(acc.lanes[0]), l1 = warp_or64(acc.lanes[1]);
   if (lane == 0) {
     s_red[0][wib] = a;
     s_red[1][wib] = b;
@@ -537,6 +543,7 @@ struct MsState {
   int32_t *pair_u = nullptr;
   uint64_t *pair_m = nullptr;
   uint8_t *pair_n = nullptr;
+  uint32_t *lightfin = nullptr;  // [2][words]: the light map, then the finished map
   int64_t bcap = 0;
   int nhub = 0;
   int lane_words = 0;
@@ -572,6 +579,8 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.pair_u = s->pair_u;
   p.pair_m = s->pair_m;
   p.pair_n = s->pair_n;
+  p.light = s->lightfin;
+  p.fin = s->lightfin ? s->lightfin + p.words : nullptr;
   p.touched0 = s->touched;
   p.scanmap = s->touched + 3 * p.words;
   p.dead = g->dead;

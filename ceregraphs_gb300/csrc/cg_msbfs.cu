@@ -648,6 +648,7 @@ static void ms_free_state(MsState *s) {
   cudaFree(s->pair_u);
   cudaFree(s->pair_m);
   cudaFree(s->pair_n);
+  cudaFree(s->lightfin);
   delete s;
 }
 
@@ -766,6 +767,23 @@ __global__ void slot_map_kernel(int count, const int32_t *__restrict__ vtx, int3
     slot[vtx[i]] = i;
 }
 
+// Bit v of light[w]: vertex v = 32 w + b has in-degree 1 .. kPullLight (the
+// vertices a ledger pull round scans one thread each).
+__global__ void light_map_kernel(int64_t n, int64_t words, const int64_t *__restrict__ in_off,
+                                 uint32_t *light) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    for (int b = 0; b < 32; ++b) {
+      const int64_t v = w * 32 + b;
+      if (v >= n) break;
+      const int64_t d = in_off[v + 1] - in_off[v];
+      if (d >= 1 && d <= kPullLight) m |= 1u << b;
+    }
+    light[w] = m;
+  }
+}
+
 // Parent-candidate slots of the output pass of a ledger batch: every vertex of
 // in-degree > kPullLight (the medium list, then the hubs) gets a slot of 64 W
 // candidates and its in-list is cut into kHubChunk-entry chunks.
@@ -780,9 +798,18 @@ static int ms_build_cands(cg_graph *g, MsState *s) {
       cudaMalloc(&s->pair_u, sizeof(int32_t) * kRecords * (size_t)g->n) != cudaSuccess ||
       cudaMalloc(&s->pair_m, sizeof(uint64_t) * kRecords * (size_t)g->n * s->lane_words) !=
           cudaSuccess ||
-      cudaMalloc(&s->pair_n, (size_t)((g->n + 3) / 4) * 4) != cudaSuccess)
+      cudaMalloc(&s->pair_n, (size_t)((g->n + 3) / 4) * 4) != cudaSuccess ||
+      cudaMalloc(&s->lightfin, sizeof(uint32_t) * 2 * (size_t)((g->n + 31) / 32)) != cudaSuccess)
     return CG_ERR_OUT_OF_MEMORY;
-  g->device_bytes += (sizeof(int32_t) + sizeof(uint64_t) * s->lane_words) * kRecords * g->n + g->n;
+  g->device_bytes += (sizeof(int32_t) + sizeof(uint64_t) * s->lane_words) * kRecords * g->n + g->n +
+                     sizeof(uint32_t) * 2 * ((g->n + 31) / 32);
+  {
+    const int64_t words = (g->n + 31) / 32;
+    const int64_t blocks = (words + 255) / 256;
+    light_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, g->stream>>>(
+        g->n, words, g->in_off, s->lightfin);
+    CG_CUDA(cudaGetLastError());
+  }
   CG_CUDA(cudaMemsetAsync(s->cand_slot, 0xff, sizeof(int32_t) * (size_t)g->n, g->stream));
   if (s->nmed)
     CG_CUDA(cudaMemcpyAsync(s->cand_vtx, s->med_vtx, sizeof(int32_t) * (size_t)s->nmed,

@@ -266,16 +266,40 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
     unsigned nextitem = 0;
     if (lane == 0) nextitem = nwarps + atomicAdd(&Rc->work, 1u);
     if (item < nlg) {
-      const int64_t b1 = min((int64_t)(item + 1) * 32 * kLightGrab, p.n);
-      for (int64_t base = (int64_t)item * 32 * kLightGrab; base < b1; base += 32) {
-        const int64_t v = base + lane;
+      // the light vertices of kLightGrab words not yet finished, compacted 32
+      // at a time (vertices without in-edges are not light: none can reach
+      // them).  Lane j < kLightGrab holds word j; the t-th vertex is the
+      // (t - prefix)-th set bit of the first word whose inclusive count
+      // exceeds t.  Only this warp touches these words of fin this round.
+      const int64_t w0 = (int64_t)item * kLightGrab;
+      uint32_t finw = 0, mine = 0;
+      if (lane < kLightGrab && w0 + lane < p.words) {
+        finw = p.fin[w0 + lane];
+        mine = __ldg(p.light + w0 + lane) & ~finw;
+      }
+      const uint32_t fin0 = finw;
+      const int cnt = __popc(mine);
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < kLightGrab; o <<= 1) {
+        const int t = __shfl_up_sync(kMsFull, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int total = __shfl_sync(kMsFull, incl, kLightGrab - 1);
+      for (int b0 = 0; b0 < total; b0 += 32) {
+        const int t = b0 + lane;
+        int wsel = 0;
+#pragma unroll
+        for (int step = kLightGrab / 2; step > 0; step >>= 1)
+          if (__shfl_sync(kMsFull, incl, wsel + step - 1) <= t) wsel += step;
+        const uint32_t wbits = __shfl_sync(kMsFull, mine, wsel);
+        const int before = __shfl_sync(kMsFull, incl - cnt, wsel);
+        const bool has = t < total;
+        int64_t v = 0;
         Mask<W> want = Mask<W>::zero();
         int64_t s = 0, e = 0;
-        // after round 0 a vertex without in-edges is in no frontier and wants
-        // nothing it could find (round 0 may still hold such a root)
-        const uint32_t dw = L > 0 && p.dead ? __ldg(p.dead + (base >> 5)) : 0u;
-        if (dw == kMsFull) continue;
-        if (v < p.n && !((dw >> lane) & 1u)) {
+        if (has) {
+          v = (w0 + wsel) * 32 + (__fns(wbits, 0, t - before + 1) & 31);
           const Mask<W> fv = ld_mask<W>(cur, v);
           const Mask<W> seen = ld_mask<W>(p.vis, v) | fv;
           if (fv.any()) st_mask<W>(p.vis, v, seen);
@@ -283,26 +307,42 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
           if (want.any()) {
             s = __ldg(p.in_off + v);
             e = __ldg(p.in_off + v + 1);
-            if (e - s > kPullLight) want = Mask<W>::zero();  // medium list or hub chunks
           }
         }
-        if (!__ballot_sync(kMsFull, want.any())) continue;
-        Mask<W> got = Mask<W>::zero();
-        bool over = false;
-        if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur, over);
-        const unsigned om = __ballot_sync(kMsFull, over);
-        if (lane == 0 && om) atomicOr(p.scanmap + (base >> 5), om);
-        const bool claimed = got.any();
+        // every running lane visited: no lane can reach v again (finished
+        // lanes never run again), so later rounds skip it
+        const bool done = has && !want.any();
+        bool claimed = false, over = false;
         int64_t deg = 0;
-        if (claimed) {
-          st_mask<W>(nxt, v, got);
-          acc_lanes<W>(acc, got);
-          deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+        if (__ballot_sync(kMsFull, want.any())) {
+          Mask<W> got = Mask<W>::zero();
+          if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur, over);
+          claimed = got.any();
+          if (claimed) {
+            st_mask<W>(nxt, v, got);
+            acc_lanes<W>(acc, got);
+            deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+          }
         }
-        const unsigned cm = __ballot_sync(kMsFull, claimed);
-        if (lane == 0 && cm) atomicOr(tnext + (base >> 5), cm);
+        // per word of the batch: claim bits (T_{L+1}), records overflow
+        // (scanmap), finished bits
+        const unsigned mybit = 1u << (unsigned)(v & 31);
+        const int wlo = __shfl_sync(kMsFull, wsel, 0);
+        const int whi = __shfl_sync(kMsFull, wsel, min(31, total - 1 - b0));
+        for (int j = wlo; j <= whi; ++j) {  // uniform: the whole warp
+          const bool inj = has && wsel == j;
+          const unsigned cb = __reduce_or_sync(kMsFull, inj && claimed ? mybit : 0u);
+          const unsigned ob = __reduce_or_sync(kMsFull, inj && over ? mybit : 0u);
+          const unsigned db = __reduce_or_sync(kMsFull, inj && done ? mybit : 0u);
+          if (lane == j) {
+            finw |= db;
+            if (cb) atomicOr(tnext + w0 + j, cb);
+            if (ob) atomicOr(p.scanmap + w0 + j, ob);
+          }
+        }
         ms_enqueue<false>(claimed, (int32_t)v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
       }
+      if (finw != fin0) p.fin[w0 + lane] = finw;
     } else if (item < nlg + nmg) {
       const unsigned mi = item - nlg;
       const int64_t j0 = (int64_t)mi * kMedGrab;
@@ -315,7 +355,12 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       int64_t sq = 0, eq = 0;
       if (W == 1 && lane < j1 - j0) {
         vq = p.med_vtx[j0 + lane];
-        wq = active.andnot(ld_mask<W>(p.vis, vq) | ld_mask<W>(cur, vq));
+        // F_L joins vis here for medium vertices (the light loop does it
+        // for light ones, the hub merge for hubs)
+        const Mask<W> fq = ld_mask<W>(cur, vq);
+        const Mask<W> sq0 = ld_mask<W>(p.vis, vq) | fq;
+        if (fq.any()) st_mask<W>(p.vis, vq, sq0);
+        wq = active.andnot(sq0);
         sq = __ldg(p.in_off + vq);
         eq = __ldg(p.in_off + vq + 1);
       }
@@ -336,7 +381,11 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
           e = __shfl_sync(kMsFull, eq, t);
         } else {
           v = p.med_vtx[j];
-          want = active.andnot(ld_mask<W>(p.vis, v) | ld_mask<W>(cur, v));
+          const Mask<W> fvm = ld_mask<W>(cur, v);
+          const Mask<W> svm = ld_mask<W>(p.vis, v) | fvm;
+          __syncwarp();
+          if (lane == 0 && fvm.any()) st_mask<W>(p.vis, v, svm);
+          want = active.andnot(svm);
           if (!want.any()) continue;
           s = __ldg(p.in_off + v);
           e = __ldg(p.in_off + v + 1);
@@ -395,7 +444,8 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
 // After the wait that ends a pull round's scans: hubs found this round get
 // their next mask and claim bit, and are queued if big.
 template <int W>
-__device__ void lg_hub_merge(const MsParams &p, int L, uint64_t *nxt, MsRound *Rn, MsAcc &acc) {
+__device__ void lg_hub_merge(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
+                             MsRound *Rn, MsAcc &acc) {
   const int lane = lane_id();
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int next_parity = (L + 1) & 1;
@@ -408,9 +458,13 @@ __device__ void lg_hub_merge(const MsParams &p, int L, uint64_t *nxt, MsRound *R
     int32_t v = 0;
     int64_t deg = 0;
     if (h < p.nhub) {
+      // F_L joins vis for the hubs (their chunk scans have ended)
+      const int32_t vh = p.hub_vtx[h];
+      const Mask<W> fh = ld_mask<W>(cur, vh);
+      if (fh.any()) st_mask<W>(p.vis, vh, ld_mask<W>(p.vis, vh) | fh);
       const Mask<W> found = ld_mask<W>(p.hub_found, h);
       if (found.any()) {
-        v = p.hub_vtx[h];
+        v = vh;
         st_mask<W>(nxt, v, found);
         st_mask<W>(p.hub_found, h, Mask<W>::zero());
         atomicOr(tnext + (v >> 5), 1u << (v & 31));
@@ -754,6 +808,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     p.touched1[w] = 0;
     p.touched2[w] = 0;
     p.scanmap[w] = 0;
+    p.fin[w] = 0;
   }
   uint32_t *pn = reinterpret_cast<uint32_t *>(p.pair_n);
   for (int64_t w = gtid; w < (p.n + 3) / 4; w += nthreads) pn[w] = 0;
@@ -821,7 +876,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
       lg_pull<W>(p, L, cur, nxt, active, Rc, Rn, acc);
       if (p.nhub > 0) {
         if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
-        lg_hub_merge<W>(p, L, nxt, Rn, acc);
+        lg_hub_merge<W>(p, L, cur, nxt, Rn, acc);
       }
     } else {
       lg_push<W>(p, L, cur, nxt, Rc, Rn, acc);
