@@ -53,11 +53,16 @@ namespace {
 constexpr int kOutBlock = 128;                 // output pass: 4 warps a block
 constexpr int kOutWarps = kOutBlock / 32;
 constexpr int kOutLevels = 4;                  // levels resolved per in-list scan
-// A warp's shared tile: 32 rows of 64 parents, lane l of row t at column
-// l ^ t (each of the warp's threads reads its own row at the same lane: no
-// bank conflicts); then 32 rows of kRecords record sources, stride kPuStride.
-constexpr int kPuStride = 9;
-constexpr int kOutWarpBytes = 32 * 64 * 4 + 32 * kPuStride * 4;
+// A warp's shared tile: one parent table of kTab words per thread -- 64
+// parents of its vertex (lane l at column (l - 8 t) mod 64 for thread t: the
+// 32 threads reading the same lane hit 32 different banks, the stride being
+// 9 mod 32), then the sources of its kRecords records at kTabRec + q, and -1
+// (unreached) at kTabNone.  A lane's parent is one table read at a byte index.
+constexpr int kTabRec = 64;
+constexpr int kTabNone = kTabRec + 8;
+constexpr int kTab = kTabNone + 1;
+constexpr int kOutWarpBytes = 32 * kTab * 4;
+static_assert(kRecords <= 8, "record indices are 3 bit slices");
 constexpr int kSlices = 7;                     // bit slices of a level (levels 0..64)
 
 // Bits 0..3 of x moved to bit 0 of bytes 0..3 (the four shifted copies do not
@@ -250,6 +255,8 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   uint32_t *boff = next_parity ? p.bigoff1 : p.bigoff0;
   uint32_t *tnext = claims(p, L + 1);
   const int lane = lane_id();
+  // a symmetric graph stores one list per vertex: out-degree = in-degree
+  const bool sym = p.out_off == p.in_off;
   // light vertex groups (kLightGrab x 32 vertices), then medium vertices
   // (groups of kMedGrab), then hub chunks (groups of kHubGrab), handed out
   // dynamically -- one item per warp, then a counter -- so that the round's
@@ -321,7 +328,7 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
           if (claimed) {
             st_mask<W>(nxt, v, got);
             acc_lanes<W>(acc, got);
-            deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+            deg = sym ? e - s : __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
           }
         }
         // per word of the batch: claim bits (T_{L+1}), records overflow
@@ -353,6 +360,7 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
       int32_t vq = 0;
       Mask<W> wq = Mask<W>::zero();
       int64_t sq = 0, eq = 0;
+      bool cq = false;  // 64 lanes: lane t's vertex was claimed (queued once, at the end)
       if (W == 1 && lane < j1 - j0) {
         vq = p.med_vtx[j0 + lane];
         // F_L joins vis here for medium vertices (the light loop does it
@@ -398,9 +406,19 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
           st_mask<W>(nxt, v, got);
           atomicOr(tnext + (v >> 5), 1u << (v & 31));
           acc_lanes<W>(acc, got);
-          deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
+          if (W != 1) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
         }
-        ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+        if (W == 1) {
+          if (lane == t && got.any()) cq = true;
+        } else {
+          ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
+        }
+      }
+      // the group's claimed vertices queued together: one atomic, not one each
+      if (W == 1) {
+        const int64_t dq =
+            !cq ? 0 : (sym ? eq - sq : __ldg(p.out_off + vq + 1) - __ldg(p.out_off + vq));
+        ms_enqueue<false>(cq, vq, dq, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
       }
     } else {
       const unsigned hi_item = item - nlg - nmg;
@@ -1000,7 +1018,7 @@ __device__ __forceinline__ void scan_in_list(const MsParams &p, int64_t v, int h
   }
 }
 
-// OR of the masks of records [0, np) of vertex v, half h.
+// OR of the masks of records [0, np) of vertex v, half h (np <= kRecords).
 template <int W>
 __device__ __forceinline__ uint64_t records_mask(const MsParams &p, int64_t v, int h, int np) {
   uint64_t m = 0;
@@ -1106,7 +1124,7 @@ __global__ void __launch_bounds__(kScanBlock, W == 1 ? 6 : 4) msbfs_fixup(MsPara
   for (int64_t i = warp_id_global(); i < cnt; i += nwarps) {
     const int64_t v = p.queue0[i];
     const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
-    const int np = p.pair_n[v];
+    const int np = min((int)p.pair_n[v], kRecords);
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
       // the lanes no record covers; those reached at a level >= 2 get parents
       uint64_t todo = ~records_mask<W>(p, v, h, np);
@@ -1145,11 +1163,12 @@ __global__ void __launch_bounds__(kScanBlock, W == 1 ? 6 : 4) msbfs_fixup(MsPara
 // 64-lane half of the batch a thread reads its vertex's history masks once
 // and keeps each lane's level as bit slices in registers; parents of levels
 // >= 2 come from the slot's candidates (in-degree > kPullLight), copied by
-// the warp into the vertex's shared tile row, or from the vertex's (source,
-// lanes) records: their sources in a shared table, each lane's record index
-// as bit slices like the levels.  Then, lane by lane,
-// the warp writes the tile's 32 levels and 32 parents as two 128-byte rows;
-// parents of levels 0 and 1 are the vertex and the lane's root.
+// the warp into the parent row of the vertex's shared table, or from the
+// vertex's (source, lanes) records: their sources in the same table, each
+// lane's record index as bit slices like the levels.  Then, lane by lane,
+// the warp writes the tile's 32 levels and 32 parents as two 128-byte rows,
+// each parent one table read; parents of levels 0 and 1 are the vertex and
+// the lane's root.
 template <int W>
 __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   extern __shared__ __align__(16) unsigned char s_tile[];
@@ -1169,17 +1188,32 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
   __syncthreads();
   const int lane = lane_id();
   const int wib = threadIdx.x >> 5;
-  int32_t *par = reinterpret_cast<int32_t *>(s_tile + wib * kOutWarpBytes);
-  int32_t *my_row = par + lane * 64;  // lane l at my_row[l ^ lane]
-  int32_t *my_pu = par + 32 * 64 + lane * kPuStride;
+  int32_t *tab = reinterpret_cast<int32_t *>(s_tile + wib * kOutWarpBytes);
+  int32_t *my_tab = tab + lane * kTab;  // lane l at my_tab[(l - 8 * lane) & 63]
+  my_tab[kTabNone] = -1;
   int nsl = 1;  // bit slices needed for levels 0 .. rounds - 1
   while (nsl < kSlices && (rounds - 1) >> nsl) ++nsl;
   const int64_t nwarps = (int64_t)gridDim.x * kOutWarps;
-  for (int64_t tile = (int64_t)blockIdx.x * kOutWarps + wib; tile * 32 < p.n; tile += nwarps) {
+  // a tile's slot and record count are loaded one tile ahead: the tile's
+  // history, candidate and record loads then all go out at its start
+  int64_t tile = (int64_t)blockIdx.x * kOutWarps + wib;
+  int next_slot = -1, next_np = 0;
+  if (tile * 32 + lane < p.n) {
+    next_slot = p.cand_slot[tile * 32 + lane];
+    next_np = p.pair_n[tile * 32 + lane];
+  }
+  for (; tile * 32 < p.n; tile += nwarps) {
     const int64_t v = tile * 32 + lane;
     const bool valid = v < p.n;
-    const int slot = valid ? p.cand_slot[v] : -1;
-    const int np = valid && slot < 0 ? p.pair_n[v] : 0;
+    const int slot = next_slot;
+    const int np = slot < 0 ? min(next_np, kRecords) : 0;
+    const int64_t vn = (tile + nwarps) * 32 + lane;
+    next_slot = -1;
+    next_np = 0;
+    if (vn < p.n) {
+      next_slot = p.cand_slot[vn];
+      next_np = p.pair_n[vn];
+    }
 #pragma unroll 1
     for (int h = 0; h < W && 64 * h < p.k; ++h) {
       // the first kPre history planes: independent of the slot and record
@@ -1211,8 +1245,9 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
             if (src[r] >= 0) {
-              par[src[r] * 64 + ((2 * lane) ^ src[r])] = (int32_t)x[r].x;
-              par[src[r] * 64 + ((2 * lane + 1) ^ src[r])] = (int32_t)x[r].y;
+              int32_t *t = tab + src[r] * kTab + ((2 * lane - 8 * src[r]) & 63);
+              t[0] = (int32_t)x[r].x;
+              t[1] = (int32_t)x[r].y;
             }
           }
         }
@@ -1236,7 +1271,7 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
         }
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-          if (q0 + r < np) my_pu[q0 + r] = pu[r];
+          if (q0 + r < np) my_tab[kTabRec + q0 + r] = pu[r];
         const uint64_t all4 = pmk[0] | pmk[1] | pmk[2] | pmk[3];
         cov |= all4;
         rq[0] |= pmk[1] | pmk[3];
@@ -1276,18 +1311,18 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
       }
       __syncwarp();  // the candidate rows copied by the warp are in place
       // levels 0 and 1 (rare): the vertex itself, the lane's root
-      for (uint64_t x = m01[0]; x; x &= x - 1) my_row[(__ffsll((long long)x) - 1) ^ lane] = (int32_t)v;
+      for (uint64_t x = m01[0]; x; x &= x - 1)
+        my_tab[(__ffsll((long long)x) - 1 - 8 * lane) & 63] = (int32_t)v;
       for (uint64_t x = m01[1]; x; x &= x - 1) {
         const int b = __ffsll((long long)x) - 1;
-        my_row[b ^ lane] = p.roots[64 * h + b];
+        my_tab[(b - 8 * lane) & 63] = p.roots[64 * h + b];
       }
       __syncwarp();
       // rows: lane l of this half, vertices tile*32 .. tile*32 + 31, a 32-lane
       // word of the masks at a time; four lanes' levels are built as the
       // bytes of a word (0xFF unreached, which sign-extends to -1)
       const int lanes = min(64, p.k - 64 * h);
-      int32_t *base_l = p.levels + v;
-      int32_t *base_p = p.parents + v;
+      const int64_t n = p.n;
 #pragma unroll 1
       for (int hw = 0; hw < 2 && 32 * hw < lanes; ++hw) {
         uint32_t sl[kSlices];
@@ -1299,31 +1334,42 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
 #pragma unroll
         for (int b = 0; b < 3; ++b) qs[b] = (uint32_t)(rq[b] >> (32 * hw));
         const int lend = min(32, lanes - 32 * hw);
+        // rows of lane 64 h + 32 hw, advanced one row per lane written
+        int32_t *pl = p.levels + (int64_t)(64 * h + 32 * hw) * n + v;
+        int32_t *pp = p.parents + (int64_t)(64 * h + 32 * hw) * n + v;
         auto group = [&](int l4, auto checked) {
-          uint32_t word = spread4(~(rw >> l4) & 0xFu) * 0xFFu;
+          // bytes of four lanes: 0xFF where unreached (um), where a record
+          // covers the lane (cm), its level (0xFF unreached sign-extends to -1)
+          const uint32_t um = spread4(~(rw >> l4) & 0xFu) * 0xFFu;
+          const uint32_t cm = spread4((cw >> l4) & 0xFu) * 0xFFu;
+          uint32_t word = um;
 #pragma unroll
           for (int b = 0; b < kSlices; ++b)
             if (b < nsl) word |= spread4((sl[b] >> l4) & 0xFu) << b;
-          // four lanes' record indices, bytes of a word as the levels
+          // each lane's table index: its record's source, -1 when unreached,
+          // else its column of the parent row ((l - 8 lane) mod 64 never
+          // wraps inside an aligned group of four)
           const uint32_t qw = spread4((qs[0] >> l4) & 0xFu) | (spread4((qs[1] >> l4) & 0xFu) << 1) |
                               (spread4((qs[2] >> l4) & 0xFu) << 2);
-          const uint32_t cq = cw >> l4;
+          const uint32_t col = ((uint32_t)((32 * hw + l4 - 8 * lane) & 63) * 0x01010101u) | 0x03020100u;
+          const uint32_t idx = (col & ~(cm | um)) | ((qw | (0x01010101u * kTabRec)) & cm) |
+                               ((0x01010101u * kTabNone) & um);
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             if (!decltype(checked)::value || l4 + i < lend) {
-              const int l = 32 * hw + l4 + i;
               const int32_t lv = (int32_t)(int8_t)(uint8_t)(word >> (8 * i));
-              const int32_t pv =
-                  (cq >> i) & 1u ? my_pu[(qw >> (8 * i)) & 0xFFu] : my_row[l ^ lane];
-              const int64_t row = (int64_t)(64 * h + l) * p.n;
+              const int32_t pv = my_tab[(idx >> (8 * i)) & 0xFFu];
               if (valid) {
-                base_l[row] = lv;
-                base_p[row] = lv < 0 ? -1 : pv;
+                *pl = lv;
+                *pp = pv;
               }
+              pl += n;
+              pp += n;
             }
           }
         };
         if (lend == 32) {
+#pragma unroll
           for (int l4 = 0; l4 < 32; l4 += 4) group(l4, Flag<false>{});
         } else {
           for (int l4 = 0; l4 < lend; l4 += 4) group(l4, Flag<true>{});
