@@ -15,7 +15,8 @@ constexpr int kMsMaxLanes = 128;
 constexpr int kPullLight = 32;    // in-degree <= this: one thread scans the in-list
 constexpr int kHubDeg = 1024;     // in-degree > this: hub
 constexpr int kHubChunk = 1024;   // in-list entries of a hub per work item
-constexpr int kPairs = 4;         // first-hit records a light vertex's pull rounds may take
+constexpr int kPairs = 8;         // first-hit records a light vertex's pull rounds may take
+                                  // (all of them: pull rounds also record push-level parents)
 constexpr int kRecords = 8;       // records per light vertex in all (pull rounds + scan pass)
 
 struct MsRound {

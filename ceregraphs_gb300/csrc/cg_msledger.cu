@@ -101,38 +101,50 @@ __device__ __forceinline__ Mask<W> or_thread(const MsParams &p, int64_t s, int64
 // or_thread that also records, for light vertex v, each in-list entry that
 // brings new lanes -- their lowest-index parent, the scan being ascending --
 // as a (source, lanes) pair, up to kPairs per vertex over all pull rounds.
-// Lanes found after the records run out (`over`) are left to the scan pass.
+// `want1`, after a push round: the lanes that push gave v at this round's
+// level L, whose parents are the first entries holding them in F_{L-1}
+// (`prev`) -- found in the same pass and recorded alike, so the scan pass
+// need not rescan v.  Lanes found after the records run out (`over`) are
+// left to the scan pass.  Returns the lanes of `want` found.
 template <int W>
 __device__ __forceinline__ Mask<W> or_thread_rec(const MsParams &p, int64_t v, int64_t s,
                                                  int64_t e, const Mask<W> &want,
-                                                 const uint64_t *cur, bool &over) {
+                                                 const uint64_t *cur, const uint64_t *prev,
+                                                 const Mask<W> &want1, bool &over) {
   constexpr int G = 4;
-  Mask<W> got = Mask<W>::zero();
+  Mask<W> got = Mask<W>::zero(), got1 = Mask<W>::zero();
+  const bool two = want1.any();
   int used = p.pair_n[v];
   const int first = used;
   for (int64_t i0 = s; i0 < e; i0 += G) {
     int32_t u[G];
-    Mask<W> m[G];
+    Mask<W> m[G], m1[G];
 #pragma unroll
     for (int k = 0; k < G; ++k) u[k] = i0 + k < e ? __ldg(p.in_idx + i0 + k) : -1;
 #pragma unroll
-    for (int k = 0; k < G; ++k) m[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+    for (int k = 0; k < G; ++k) {
+      m[k] = u[k] >= 0 ? ld_mask<W>(cur, u[k]) : Mask<W>::zero();
+      m1[k] = two && u[k] >= 0 ? ld_mask<W>(prev, u[k]) : Mask<W>::zero();
+    }
 #pragma unroll
     for (int k = 0; k < G; ++k) {
       const Mask<W> nb = (m[k] & want).andnot(got);
-      if (nb.any()) {
+      const Mask<W> nb1 = (m1[k] & want1).andnot(got1);
+      const Mask<W> r = nb | nb1;  // disjoint: want1 lanes are visited, want lanes are not
+      if (r.any()) {
         if (used < kPairs) {
           const int64_t at = (int64_t)used * p.n + v;
           p.pair_u[at] = u[k];
-          st_mask<W>(p.pair_m, at, nb);
+          st_mask<W>(p.pair_m, at, r);
           ++used;
         } else {
           over = true;
         }
         got = got | nb;
+        got1 = got1 | nb1;
       }
     }
-    if (got == want) break;
+    if (got == want && got1 == want1) break;
   }
   if (used != first) p.pair_n[v] = (uint8_t)used;
   return got;
@@ -248,7 +260,13 @@ __device__ __forceinline__ uint32_t *claims(const MsParams &p, int L) {
 // hub in-lists by chunks (ORed into hub_found, merged after the wait).
 template <int W>
 __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
-                        const Mask<W> &active, MsRound *Rc, MsRound *Rn, MsAcc &acc) {
+                        const Mask<W> &active, bool after_push, MsRound *Rc, MsRound *Rn,
+                        MsAcc &acc) {
+  // after a push round of level >= 1, light vertices also resolve the
+  // parents of the lanes that push gave them (F_L) against F_{L-1} (64
+  // lanes; with 128 the registers would spill, and the scan pass does it)
+  after_push = after_push && W == 1;
+  const uint64_t *prev = after_push ? plane<W>(p, L - 1) : cur;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   const int next_parity = (L + 1) & 1;
   int32_t *q = next_parity ? p.queue1 : p.queue0;
@@ -303,7 +321,7 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         const int before = __shfl_sync(kMsFull, incl - cnt, wsel);
         const bool has = t < total;
         int64_t v = 0;
-        Mask<W> want = Mask<W>::zero();
+        Mask<W> want = Mask<W>::zero(), want1 = Mask<W>::zero();
         int64_t s = 0, e = 0;
         if (has) {
           v = (w0 + wsel) * 32 + (__fns(wbits, 0, t - before + 1) & 31);
@@ -311,7 +329,8 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
           const Mask<W> seen = ld_mask<W>(p.vis, v) | fv;
           if (fv.any()) st_mask<W>(p.vis, v, seen);
           want = active.andnot(seen);
-          if (want.any()) {
+          if (after_push) want1 = fv;
+          if (want.any() || want1.any()) {
             s = __ldg(p.in_off + v);
             e = __ldg(p.in_off + v + 1);
           }
@@ -321,9 +340,10 @@ __device__ void lg_pull(const MsParams &p, int L, const uint64_t *cur, uint64_t 
         const bool done = has && !want.any();
         bool claimed = false, over = false;
         int64_t deg = 0;
-        if (__ballot_sync(kMsFull, want.any())) {
+        const bool scan = want.any() || want1.any();
+        if (__ballot_sync(kMsFull, scan)) {
           Mask<W> got = Mask<W>::zero();
-          if (want.any()) got = or_thread_rec<W>(p, v, s, e, want, cur, over);
+          if (scan) got = or_thread_rec<W>(p, v, s, e, want, cur, prev, want1, over);
           claimed = got.any();
           if (claimed) {
             st_mask<W>(nxt, v, got);
@@ -877,10 +897,10 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     }
     uint32_t *tclr = claims(p, L + 2);
     for (int64_t w = gtid; w < p.words; w += nthreads) tclr[w] = 0;
-    if (L >= 2 && pdir == 0) {
-      // a push round gave these vertices lanes at level L >= 2: the scan
-      // pass resolves their parents (atomic: a pull round of this same
-      // round L may mark vertices of the same words)
+    if (L >= 2 && pdir == 0 && (dir == 0 || W != 1)) {
+      // a push round gave these vertices lanes at level L >= 2 and this
+      // round is a push too (or 128 lanes): the scan pass resolves their
+      // parents (else this pull round's light scans do, or_thread_rec)
       const uint32_t *tcur = claims(p, L);
       for (int64_t w = gtid; w < p.words; w += nthreads) {
         const uint32_t t = tcur[w];
@@ -891,7 +911,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
       Mask<W> active;
 #pragma unroll
       for (int i = 0; i < W; ++i) active.w[i] = *(volatile unsigned long long *)&Rc->lanes[i];
-      lg_pull<W>(p, L, cur, nxt, active, Rc, Rn, acc);
+      lg_pull<W>(p, L, cur, nxt, active, L >= 2 && pdir == 0, Rc, Rn, acc);
       if (p.nhub > 0) {
         if (!(ok = grid_wait(&ctl->wait, &ctl->status, p.timeout_ns))) break;
         lg_hub_merge<W>(p, L, cur, nxt, Rn, acc);
