@@ -1379,9 +1379,9 @@ __global__ void __launch_bounds__(kOutBlock) msbfs_outputs(MsParams p) {
             if (!decltype(checked)::value || l4 + i < lend) {
               const int32_t lv = (int32_t)(int8_t)(uint8_t)(word >> (8 * i));
               const int32_t pv = my_tab[(idx >> (8 * i)) & 0xFFu];
-              if (valid) {
-                *pl = lv;
-                *pp = pv;
+              if (valid) {  // written once, never read here: evict-first
+                __stcs(pl, lv);
+                __stcs(pp, pv);
               }
               pl += n;
               pp += n;
