@@ -517,7 +517,8 @@ __device__ __forceinline__ void ms_block_totals(MsAcc &acc, MsAcc &tot) {
   acc = MsAcc();
 }
 
-constexpr unsigned kMsStop = 1u, kMsNextPull = 2u;
+// kMsSparse (ledger): the next round's frontier has under n/1024 vertices
+constexpr unsigned kMsStop = 1u, kMsNextPull = 2u, kMsSparse = 4u;
 
 struct MsState {
   uint64_t *bits = nullptr;

@@ -519,17 +519,20 @@ __device__ void lg_hub_merge(const MsParams &p, int L, const uint64_t *cur, uint
 // visited nor in its own frontier of this round are ORed into v's next mask
 // (after a read, so hot targets see few atomics); a vertex with a candidate
 // slot also takes u as a parent candidate per lane (atomicMin).  The loads
-// that depend only on v go out together.  Returns whether this thread
-// claimed v (set its bit in the next claim bitmap first).
+// that depend only on v go out together; with a sparse frontier (`tfront`,
+// its claim bitmap) v's own frontier mask is read only if v is in it.
+// Returns whether this thread claimed v (set its bit in the next claim
+// bitmap first).
 template <int W>
 __device__ __forceinline__ bool lg_relax(const MsParams &p, const Mask<W> &fu, int32_t u,
                                          int32_t v, const uint64_t *cur, uint64_t *nxt,
-                                         uint32_t *tnext, MsAcc &acc) {
+                                         uint32_t *tnext, const uint32_t *tfront, MsAcc &acc) {
   const Mask<W> seen = ld_mask<W>(p.vis, v);
-  const Mask<W> now = ld_mask<W>(cur, v);
   const Mask<W> have = ld_mask<W>(nxt, v);
   const int slot = p.cand_slot[v];
   const uint32_t tw = tnext[v >> 5];
+  Mask<W> now = Mask<W>::zero();
+  if (!tfront || ((tfront[v >> 5] >> (v & 31)) & 1u)) now = ld_mask<W>(cur, v);
   const Mask<W> f = fu.andnot(seen | now);
   if (!f.any()) return false;
   acc_lanes<W>(acc, f);
@@ -570,14 +573,14 @@ __device__ __forceinline__ bool lg_relax(const MsParams &p, const Mask<W> &fu, i
 template <int W>
 __device__ __forceinline__ void lg_step(const MsParams &p, bool valid, const Mask<W> &fu,
                                         int32_t u, int64_t e, const uint64_t *cur, uint64_t *nxt,
-                                        uint32_t *tnext, int32_t *q, uint32_t *boff, MsRound *Rn,
-                                        MsAcc &acc) {
+                                        uint32_t *tnext, const uint32_t *tfront, int32_t *q,
+                                        uint32_t *boff, MsRound *Rn, MsAcc &acc) {
   bool claimed = false;
   int32_t v = 0;
   int64_t deg = 0;
   if (valid) {
     v = __ldg(p.out_idx + e);
-    claimed = lg_relax<W>(p, fu, u, v, cur, nxt, tnext, acc);
+    claimed = lg_relax<W>(p, fu, u, v, cur, nxt, tnext, tfront, acc);
     if (claimed) deg = __ldg(p.out_off + v + 1) - __ldg(p.out_off + v);
   }
   ms_enqueue<false>(claimed, v, deg, q, p.n, boff, &Rn->nlight, &Rn->big, acc);
@@ -588,8 +591,8 @@ __device__ __forceinline__ void lg_step(const MsParams &p, bool valid, const Mas
 template <int W>
 __device__ void lg_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *nxt,
                               uint32_t *tnext, const int32_t *bq, const uint32_t *boff,
-                              unsigned nbig, unsigned x0, unsigned x1, int32_t *q, uint32_t *qoff,
-                              MsRound *Rn, MsAcc &acc) {
+                              unsigned nbig, unsigned x0, unsigned x1, const uint32_t *tfront,
+                              int32_t *q, uint32_t *qoff, MsRound *Rn, MsAcc &acc) {
   const int lane = lane_id();
   const int64_t cap = p.n;
   unsigned lo = 0, hi = nbig - 1;
@@ -628,7 +631,7 @@ __device__ void lg_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *
         fu = ld_mask<W>(cur, vn);
       }
     }
-    lg_step<W>(p, valid, fu, u, e, cur, nxt, tnext, q, qoff, Rn, acc);
+    lg_step<W>(p, valid, fu, u, e, cur, nxt, tnext, tfront, q, qoff, Rn, acc);
   }
 }
 
@@ -638,7 +641,7 @@ __device__ void lg_push_chunk(const MsParams &p, const uint64_t *cur, uint64_t *
 // light ones (out-degree <= kLightMax) spread their edges over the warp.
 template <int W>
 __device__ void lg_push(const MsParams &p, int L, const uint64_t *cur, uint64_t *nxt,
-                        MsRound *Rc, MsRound *Rn, MsAcc &acc) {
+                        bool sparse, MsRound *Rc, MsRound *Rn, MsAcc &acc) {
   __shared__ int32_t s_u[kMsBlock / 32][32];
   __shared__ int64_t s_s[kMsBlock / 32][32];
   __shared__ int64_t s_x[kMsBlock / 32][32];
@@ -652,6 +655,10 @@ __device__ void lg_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   uint32_t *bn = next_parity ? p.bigoff1 : p.bigoff0;
   const uint32_t *tcur = claims(p, L);
   uint32_t *tnext = claims(p, L + 1);
+  // a frontier of under n/1024 vertices (few targets are in it): its claim
+  // bitmap (1/64 of a mask plane, cache-resident) is tested before a
+  // target's frontier mask is read
+  const uint32_t *tfront = sparse ? tcur : nullptr;
 
   const unsigned long long bigw = *(volatile unsigned long long *)&Rc->big;
   const unsigned nbig = (unsigned)(bigw >> 32), big_edges = (unsigned)bigw;
@@ -664,8 +671,8 @@ __device__ void lg_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
   while (item < nitems) {
     if (item < nb) {
       const unsigned x0 = item * chunk;
-      lg_push_chunk<W>(p, cur, nxt, tnext, qc, bc, nbig, x0, min(x0 + chunk, big_edges), qn, bn,
-                       Rn, acc);
+      lg_push_chunk<W>(p, cur, nxt, tnext, qc, bc, nbig, x0, min(x0 + chunk, big_edges), tfront,
+                       qn, bn, Rn, acc);
     } else {
       // the group's frontier vertices, compacted 32 at a time: lane j holds
       // word j; the t-th frontier vertex is the (t - prefix)-th set bit of the
@@ -734,7 +741,7 @@ __device__ void lg_push(const MsParams &p, int L, const uint64_t *cur, uint64_t 
             fu = ld_mask<W>(cur, uu);
             e = s_s[wib][lo] + (t2 - s_x[wib][lo]);
           }
-          lg_step<W>(p, valid, fu, uu, e, cur, nxt, tnext, qn, bn, Rn, acc);
+          lg_step<W>(p, valid, fu, uu, e, cur, nxt, tnext, tfront, qn, bn, Rn, acc);
         }
         __syncwarp();
       }
@@ -801,7 +808,8 @@ __device__ unsigned lg_decide(const MsParams &p, int L, int dir, int ran) {
     st->history_len = rounds < CG_HISTORY ? rounds : CG_HISTORY;
     st->device_ms = 0.f;
   }
-  return (stop ? kMsStop : 0u) | (next ? kMsNextPull : 0u);
+  return (stop ? kMsStop : 0u) | (next ? kMsNextPull : 0u) |
+         (nf * 1024 < (unsigned long long)p.n ? kMsSparse : 0u);
 }
 
 template <int W>
@@ -885,6 +893,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     ok = s_payload != kWaitFailed;
   }
   int L = 0, dir = 0, pdir = 0, ran = 0;
+  bool sparse = false;  // this round's frontier has under n/1024 vertices (round 0: not tested)
   MsAcc acc, tot;
   while (ok) {
     const uint64_t *cur = plane<W>(p, L);
@@ -917,7 +926,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
         lg_hub_merge<W>(p, L, cur, nxt, Rn, acc);
       }
     } else {
-      lg_push<W>(p, L, cur, nxt, Rc, Rn, acc);
+      lg_push<W>(p, L, cur, nxt, sparse, Rc, Rn, acc);
     }
     ms_block_totals(acc, tot);
     if (threadIdx.x == 0) {
@@ -938,6 +947,7 @@ __global__ void __launch_bounds__(kMsBlock, 2) msbfs_ledger(MsParams p) {
     if (payload & kMsStop) break;
     pdir = dir;
     dir = (payload & kMsNextPull) ? 1 : 0;
+    sparse = (payload & kMsSparse) != 0;
     ++L;
     ++ran;
   }
@@ -1091,6 +1101,10 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
       const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
       if (e == s || e - s > kPullLight) continue;
       const int np0 = p.pair_n[v];
+      if (np0 >= kRecords) {  // no record left: the fix-up pass resolves the open lanes
+        p.queue0[atomicAdd(&p.ctl->nover, 1u)] = (int32_t)v;
+        continue;
+      }
       int np = np0;
       bool over = false;
       // the records' sources: a hit from a source already recorded joins its
