@@ -15,8 +15,9 @@ constexpr int kMsMaxLanes = 128;
 constexpr int kPullLight = 32;    // in-degree <= this: one thread scans the in-list
 constexpr int kHubDeg = 1024;     // in-degree > this: hub
 constexpr int kHubChunk = 1024;   // in-list entries of a hub per work item
-constexpr int kPairs = 8;         // first-hit records a light vertex's pull rounds may take
-                                  // (all of them: pull rounds also record push-level parents)
+constexpr int kPairs = 4;         // first-hit records a light vertex's pull rounds may take,
+                                  // unless the light vertices hold under half of the edges
+                                  // (then all kRecords: see MsState::pull_records)
 constexpr int kRecords = 8;       // records per light vertex in all (pull rounds + scan pass)
 
 struct MsRound {
@@ -74,6 +75,7 @@ struct MsParams {
   // reach them again), so later pull rounds skip them
   const uint32_t *light;
   uint32_t *fin;
+  int pull_records;    // ledger: records a light vertex's pull rounds may take (<= kRecords)
   int32_t *queue0, *queue1;
   uint32_t *bigoff0, *bigoff1;
   const int32_t *hub_slot;   // [n], -1 for non-hubs
@@ -546,6 +548,7 @@ struct MsState {
   uint64_t *pair_m = nullptr;
   uint8_t *pair_n = nullptr;
   uint32_t *lightfin = nullptr;  // [2][words]: the light map, then the finished map
+  int pull_records = kPairs;     // records a light vertex's pull rounds may take
   int64_t bcap = 0;
   int nhub = 0;
   int lane_words = 0;
@@ -583,6 +586,7 @@ inline MsParams ms_params(const cg_graph *g, const MsState *s) {
   p.pair_n = s->pair_n;
   p.light = s->lightfin;
   p.fin = s->lightfin ? s->lightfin + p.words : nullptr;
+  p.pull_records = s->pull_records;
   p.touched0 = s->touched;
   p.scanmap = s->touched + 3 * p.words;
   p.dead = g->dead;

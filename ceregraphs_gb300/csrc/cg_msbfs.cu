@@ -768,9 +768,11 @@ __global__ void slot_map_kernel(int count, const int32_t *__restrict__ vtx, int3
 }
 
 // Bit v of light[w]: vertex v = 32 w + b has in-degree 1 .. kPullLight (the
-// vertices a ledger pull round scans one thread each).
+// vertices a ledger pull round scans one thread each); *light_edges sums
+// their in-degrees.
 __global__ void light_map_kernel(int64_t n, int64_t words, const int64_t *__restrict__ in_off,
-                                 uint32_t *light) {
+                                 uint32_t *light, unsigned long long *light_edges) {
+  unsigned long long e = 0;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
        w += (int64_t)gridDim.x * blockDim.x) {
     uint32_t m = 0;
@@ -778,10 +780,14 @@ __global__ void light_map_kernel(int64_t n, int64_t words, const int64_t *__rest
       const int64_t v = w * 32 + b;
       if (v >= n) break;
       const int64_t d = in_off[v + 1] - in_off[v];
-      if (d >= 1 && d <= kPullLight) m |= 1u << b;
+      if (d >= 1 && d <= kPullLight) {
+        m |= 1u << b;
+        e += (unsigned long long)d;
+      }
     }
     light[w] = m;
   }
+  if (e) atomicAdd(light_edges, e);
 }
 
 // Parent-candidate slots of the output pass of a ledger batch: every vertex of
@@ -804,11 +810,27 @@ static int ms_build_cands(cg_graph *g, MsState *s) {
   g->device_bytes += (sizeof(int32_t) + sizeof(uint64_t) * s->lane_words) * kRecords * g->n + g->n +
                      sizeof(uint32_t) * 2 * ((g->n + 31) / 32);
   {
+    // pull rounds may take all kRecords records where light vertices hold
+    // under half of the edges (their parents are a few hubs: R-MAT), else
+    // kPairs, leaving room for the scan pass to merge later hits into
+    // records of the same source (graphs of light vertices only: each is
+    // reached over many rounds, from the same few in-neighbours)
     const int64_t words = (g->n + 31) / 32;
     const int64_t blocks = (words + 255) / 256;
-    light_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, g->stream>>>(
-        g->n, words, g->in_off, s->lightfin);
-    CG_CUDA(cudaGetLastError());
+    unsigned long long *d_le = nullptr, le = 0;
+    CG_CUDA(cudaMalloc(&d_le, sizeof(unsigned long long)));
+    cudaError_t e = cudaMemsetAsync(d_le, 0, sizeof(unsigned long long), g->stream);
+    if (e == cudaSuccess) {
+      light_map_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, g->stream>>>(
+          g->n, words, g->in_off, s->lightfin, d_le);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&le, d_le, sizeof(le), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(d_le);
+    if (e != cudaSuccess) return cuda_fail(e, "light-vertex map");
+    s->pull_records = 2 * le < (unsigned long long)g->nnz ? kRecords : kPairs;
   }
   CG_CUDA(cudaMemsetAsync(s->cand_slot, 0xff, sizeof(int32_t) * (size_t)g->n, g->stream));
   if (s->nmed)

@@ -100,7 +100,7 @@ __device__ __forceinline__ Mask<W> or_thread(const MsParams &p, int64_t s, int64
 
 // or_thread that also records, for light vertex v, each in-list entry that
 // brings new lanes -- their lowest-index parent, the scan being ascending --
-// as a (source, lanes) pair, up to kPairs per vertex over all pull rounds.
+// as a (source, lanes) pair, up to p.pull_records per vertex over all pull rounds.
 // `want1`, after a push round: the lanes that push gave v at this round's
 // level L, whose parents are the first entries holding them in F_{L-1}
 // (`prev`) -- found in the same pass and recorded alike, so the scan pass
@@ -132,7 +132,7 @@ __device__ __forceinline__ Mask<W> or_thread_rec(const MsParams &p, int64_t v, i
       const Mask<W> nb1 = (m1[k] & want1).andnot(got1);
       const Mask<W> r = nb | nb1;  // disjoint: want1 lanes are visited, want lanes are not
       if (r.any()) {
-        if (used < kPairs) {
+        if (used < p.pull_records) {
           const int64_t at = (int64_t)used * p.n + v;
           p.pair_u[at] = u[k];
           st_mask<W>(p.pair_m, at, r);
@@ -1101,10 +1101,6 @@ __global__ void __launch_bounds__(kScanBlock) msbfs_scan(MsParams p) {
       const int64_t s = __ldg(p.in_off + v), e = __ldg(p.in_off + v + 1);
       if (e == s || e - s > kPullLight) continue;
       const int np0 = p.pair_n[v];
-      if (np0 >= kRecords) {  // no record left: the fix-up pass resolves the open lanes
-        p.queue0[atomicAdd(&p.ctl->nover, 1u)] = (int32_t)v;
-        continue;
-      }
       int np = np0;
       bool over = false;
       // the records' sources: a hit from a source already recorded joins its
