@@ -711,9 +711,10 @@ def run_serving(args):
     bsrv = serving.BatchServer(graphs, lane_words=1, hbm_budget_bytes=budget, batch_min=4)
     dyn = bsrv.run(arrivals, realtime=True, time_limit=limit).summary()
     dyn["launches"] = dict(bsrv.launches)
-    srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget)
+    srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget, batch_min=8)
     pool = srv.run(arrivals, realtime=True, time_limit=limit).summary()
     pool["per_root_solo"] = srv.solo
+    pool["batched_backlog"] = srv.batched
     srv.close()
     base = serving.serial_baseline(graphs, arrivals, realtime=True, time_limit=limit).summary()
     rows.append({"rate_qps": rate, "arrivals": count, "window_s": args.serving_seconds,
@@ -734,7 +735,9 @@ def run_serving(args):
                                           "per-root), outputs written after the rounds",
                                "pool": "continuous batching: queries join searches in "
                                        "flight as bit lanes of a resumable launch; a query "
-                                       "finding its graph idle and alone runs per-root",
+                                       "finding its graph idle and alone runs per-root; an "
+                                       "idle graph's backlog of >= 8 runs as one batched "
+                                       "search",
                                "serial": "one per-root search at a time, FIFO"}},
           "e2e": {"value": best, "unit": "queries/s", "h2d_bytes_per_step": 8,
                   "d2h_bytes_per_step": 16,

@@ -145,10 +145,14 @@ def check_budget(graphs, hbm_budget_bytes):
 class Server:
   """Continuous batching over one pool per resident graph: queries join the
   searches in flight as free lanes; a query that finds its graph's pool idle
-  with no other query waiting runs as a per-root search instead."""
+  with no other query waiting runs as a per-root search instead.  With
+  `batch_min`, a backlog of at least that many waiting queries stops joining
+  the pool; once the pool is idle it starts them (up to its lanes) as one
+  batched search with outputs written after the rounds -- a backlog's cheapest
+  form -- while a shorter queue keeps joining searches in flight."""
 
   def __init__(self, graphs, lane_words=1, hbm_budget_bytes=None, max_rounds=0,
-               on_done=None, solo_max=1):
+               on_done=None, solo_max=1, batch_min=None):
     import torch
     check_budget(graphs, hbm_budget_bytes)
     self.torch = torch
@@ -158,6 +162,10 @@ class Server:
     # searches (light load: a lone query does not pay for a lane sweep)
     self.solo_max = solo_max
     self.solo = 0
+    self.batch_min = batch_min
+    self.batched = 0                          # queries served by batched searches
+    for g in graphs.values():
+      g.set_options(lane_words=int(lane_words))
     self.pools = {k: Pool(g, lane_words) for k, g in graphs.items()}
     self.budget = hbm_budget_bytes
     self.in_use = 0
@@ -204,6 +212,9 @@ class Server:
         waiting[q.graph].append(q)
       for name, pool in self.pools.items():
         wq = waiting[name]
+        if (self.batch_min and not inflight[name] and len(wq) >= self.batch_min and
+            self._batch(name, pool, wq, report, t0)):
+          continue
         if wq and not inflight[name] and len(wq) <= self.solo_max:
           g = self.graphs[name]
           while wq:
@@ -226,6 +237,8 @@ class Server:
         while wq:
           if self.budget is not None and self.in_use + self._bytes(name) > self.budget:
             break
+          if self.batch_min and len(wq) >= self.batch_min:
+            break  # a backlog waits for the pool to drain, then runs as one batch
           q = wq[0]
           lv, pa = self._buffers(name)
           lane = pool.admit(q.root, lv, pa)
@@ -262,6 +275,43 @@ class Server:
     report.wall_s = time.perf_counter() - t0
     report.queries.sort(key=lambda q: q.qid)
     return report
+
+  def _batch(self, name, pool, wq, report, t0):
+    """The waiting queries of an idle pool (up to its lanes, within the HBM
+    budget) as one batched search, run to the end; False if none fits."""
+    torch = self.torch
+    g = self.graphs[name]
+    take = min(len(wq), pool.lanes)
+    if self.budget is not None:
+      take = min(take, max(0, (self.budget - self.in_use) // self._bytes(name)))
+    if take == 0:
+      return False
+    qs = [wq.popleft() for _ in range(take)]
+    tnow = time.perf_counter() - t0
+    for q in qs:
+      q.t_admit = tnow
+    nbytes = self._bytes(name) * take
+    self.in_use += nbytes
+    lv = torch.empty((take, g.n), dtype=torch.int32, device="cuda")
+    pa = torch.empty((take, g.n), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()          # the outputs exist before the graph's stream writes them
+    g.msbfs_device([q.root for q in qs], lv, pa)
+    st = g.last_stats()               # waits for the batch
+    if st["status"] != 0:
+      raise RuntimeError(f"batched search failed: {st}")
+    tnow = time.perf_counter() - t0
+    for i, q in enumerate(qs):
+      q.t_done = tnow
+      q.levels, q.parents = lv[i], pa[i]
+      if self.on_done is not None:
+        self.on_done(q)
+      q.levels = q.parents = None
+      report.queries.append(q)
+    del lv, pa
+    self.in_use -= nbytes
+    self.batched += take
+    report.steps += 1
+    return True
 
   def close(self):
     for p in self.pools.values():

@@ -110,10 +110,11 @@ def test_pool_directed_and_deep(built_lib, oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("solo_max", [0, 1])
-def test_server_mix_equals_alone_under_hbm_budget(built_lib, solo_max):
+@pytest.mark.parametrize("solo_max,batch_min", [(0, None), (1, None), (1, 4)])
+def test_server_mix_equals_alone_under_hbm_budget(built_lib, solo_max, batch_min):
   """Queries served in the pool's mix (solo_max 0: every query through lanes;
-  1: a lone query on an idle graph runs per-root) equal their searches alone."""
+  1: a lone query on an idle graph runs per-root; batch_min 4: an idle pool's
+  backlog of 4 or more runs as one batched search) equal their searches alone."""
   import torch
   from ceregraphs_gb300.engine import Graph
   arrays = {"rmat13": generators.rmat(13, 16, 2), "rmat15": generators.rmat(15, 8, 3)}
@@ -136,7 +137,7 @@ def test_server_mix_equals_alone_under_hbm_budget(built_lib, solo_max):
 
   budget = 40 * 8 * max(a.n for a in arrays.values())
   srv = serving.Server(graphs, lane_words=1, hbm_budget_bytes=budget, on_done=on_done,
-                       solo_max=solo_max)
+                       solo_max=solo_max, batch_min=batch_min)
   orig = srv._buffers
 
   def tracked(name):
@@ -146,6 +147,7 @@ def test_server_mix_equals_alone_under_hbm_budget(built_lib, solo_max):
   rep = srv.run(arrivals, realtime=True)
   srv.close()
   assert len(rep.queries) == 300 and all(checked) and len(checked) == 300
+  assert (srv.batched > 0) == (batch_min is not None)
   assert srv.in_use == 0 and peak[0] <= budget + 8 * max(a.n for a in arrays.values())
   s = rep.summary()
   assert s["p99_ms"] >= s["p50_ms"] > 0
