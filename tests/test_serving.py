@@ -231,3 +231,92 @@ def test_time_limit_stops_admission_and_counts_the_rest(built_lib):
     assert all(q.t_done >= q.t_arrival for q in rep.queries)
   for g in graphs.values():
     g.close()
+
+
+class _FakeGraph:
+  """Host stand-in for engine.Graph: a search fills its outputs with its root."""
+
+  def __init__(self, n):
+    self.n = n
+    self.handle = None
+
+  def set_options(self, **kw):
+    pass
+
+  def bfs_device(self, root, lv, pa):
+    lv.fill_(root)
+    pa.fill_(root)
+
+  def msbfs_device(self, roots, lv, pa):
+    for i, r in enumerate(roots):
+      lv[i].fill_(r)
+      pa[i].fill_(r)
+
+  def last_stats(self):
+    return {"status": 0}
+
+
+class _FakePool:
+  """Host stand-in for serving.Pool: a lane's search ends two steps after its
+  admission and then fills its outputs with its root."""
+
+  def __init__(self, graph, lane_words=1):
+    self.lanes = 64 * int(lane_words)
+    self.live = {}
+    self.admitted = 0
+
+  def admit(self, root, lv, pa):
+    free = [l for l in range(self.lanes) if l not in self.live]
+    if not free:
+      return None
+    self.live[free[0]] = [root, lv, pa, 2]
+    self.admitted += 1
+    return free[0]
+
+  def step(self, max_rounds=0, stop_on_finish=True):
+    done = []
+    for lane, rec in self.live.items():
+      rec[3] -= 1
+      if rec[3] == 0:
+        rec[1].fill_(rec[0])
+        rec[2].fill_(rec[0])
+        done.append(lane)
+    return done
+
+  def release(self, lane):
+    del self.live[lane]
+
+  def close(self):
+    pass
+
+
+@pytest.mark.parametrize("count,solo_max,batch_min,expect", [
+    (1, 1, 4, "solo"), (10, 1, 4, "batched"), (3, 0, 4, "pool"), (70, 0, None, "pool")])
+def test_server_rules_on_the_host(monkeypatch, count, solo_max, batch_min, expect):
+  """The continuous server's admission rules with host stand-ins for the
+  pools and graphs (no GPU): a lone query on an idle graph runs per-root, a
+  backlog of batch_min or more runs as one batched search once the pool is
+  idle, a shorter queue joins the pool's lanes (more queries than lanes wait
+  for lanes to free up); every query ends with its own root's outputs."""
+  import types
+
+  import torch
+  monkeypatch.setattr(serving, "Pool", _FakePool)
+  graphs = {"g": _FakeGraph(16)}
+  seen = {}
+
+  def on_done(q):
+    seen[q.qid] = (int(q.levels[0]), int(q.parents[-1]), q.root)
+
+  srv = serving.Server(graphs, on_done=on_done, solo_max=solo_max, batch_min=batch_min)
+  srv.torch = types.SimpleNamespace(
+      empty=lambda shape, dtype=None, device=None: torch.empty(shape, dtype=dtype),
+      int32=torch.int32, cuda=types.SimpleNamespace(synchronize=lambda: None))
+  monkeypatch.setattr(torch.cuda, "synchronize", lambda: None)
+  arrivals = [(0.0, "g", 100 + i) for i in range(count)]
+  rep = srv.run(arrivals, realtime=False)
+  assert len(rep.queries) == count and srv.in_use == 0
+  assert all(lv == pa == root for lv, pa, root in seen.values()) and len(seen) == count
+  pool_admitted = srv.pools["g"].admitted
+  assert (srv.solo, srv.batched, pool_admitted) == {
+      "solo": (count, 0, 0), "batched": (0, count, 0), "pool": (0, 0, count)}[expect]
